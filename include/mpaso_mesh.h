@@ -1,0 +1,81 @@
+/*
+ * mpaso_mesh.h -- host-side mesh services of libmpaso (no GPU needed).
+ *
+ * The reference reads MPAS meshes from HDF5 files (mpasoflecsi/specialization/
+ * definition.hh:1055-1106) and computes the FCT / del2 static coefficients on
+ * the host once (apps/ocean/tasks/init_functions.cc:18-447).  HDF5 is not part
+ * of this build, so libmpaso generates the same MPAS mesh datasets in memory:
+ *
+ *   - a quasi-uniform sphere, the Voronoi dual of a recursively bisected
+ *     icosahedron (10*4^level + 2 cells);
+ *   - a doubly periodic planar hexagonal mesh (nx*ny cells).
+ *
+ * Every dataset is exposed under its MPAS name with the MPAS file conventions:
+ * connectivity is int32, 1-based, padded with 0 up to maxEdges (8) /
+ * maxEdges2 (16) / vertexDegree (3) columns; real fields are float64.
+ *
+ * All functions return 0 on success and a nonzero MPASO_ERR_* code on failure;
+ * mpaso_last_error() returns the calling thread's last message.
+ */
+#ifndef MPASO_MESH_H
+#define MPASO_MESH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPASO_OK 0
+#define MPASO_ERR_ARG 1       /* bad argument (null pointer, size out of range) */
+#define MPASO_ERR_MESH 2      /* inconsistent mesh / connectivity */
+#define MPASO_ERR_CUDA 3      /* CUDA runtime error */
+#define MPASO_ERR_ALLOC 4     /* allocation failure (host or device) */
+#define MPASO_ERR_NOTFOUND 5  /* unknown dataset name */
+#define MPASO_ERR_TIMEOUT 6   /* a bounded device-side wait gave up */
+#define MPASO_ERR_NUMERIC 7   /* non-finite value detected where checked */
+#define MPASO_ERR_NODEVICE 8  /* no CUDA device available */
+
+#define MPASO_DTYPE_INT32 0
+#define MPASO_DTYPE_FLOAT64 1
+
+typedef struct mpaso_genmesh_s *mpaso_genmesh;
+
+/* Thread-local text of the last error raised by any libmpaso call. */
+const char *mpaso_last_error(void);
+
+/* Sphere of radius `radius` (m): dual of a level-`level` icosahedral
+ * subdivision, 0 <= level <= 10.  A fixed generic rotation is applied so that
+ * no generator lies on a coordinate plane. f = 2*omega*sin(lat). */
+int mpaso_genmesh_icosa(int level, double radius, double omega, mpaso_genmesh *out);
+
+/* Doubly periodic hexagonal mesh with nx columns, ny rows (ny even, nx,ny >= 4)
+ * and cell-centre spacing dc (m); f-plane Coriolis f0 everywhere. */
+int mpaso_genmesh_hex(int nx, int ny, double dc, double f0, mpaso_genmesh *out);
+
+/* Renumber a generated mesh along a space-filling curve (cells by curve key,
+ * edges and vertices by their lowest new cell), keeping every MPAS ordering
+ * convention.  Produces a new handle; `perm_cell[new] = old` etc. if non-null. */
+int mpaso_genmesh_reorder_sfc(mpaso_genmesh in, mpaso_genmesh *out,
+                              int32_t *perm_cell, int32_t *perm_edge, int32_t *perm_vertex);
+
+/* dims[0..2] = nCells, nEdges, nVertices; flags[0] = 1 on a sphere,
+ * geom[0..2] = sphere radius, periodic x-extent, periodic y-extent. */
+int mpaso_genmesh_dims(mpaso_genmesh m, int64_t dims[3], int32_t flags[1], double geom[3]);
+
+/* Shape and element type of a named dataset. */
+int mpaso_genmesh_field(mpaso_genmesh m, const char *name, int32_t *dtype,
+                        int64_t *rows, int64_t *cols);
+
+/* Copy a named dataset (rows*cols elements) into dst. */
+int mpaso_genmesh_copy(mpaso_genmesh m, const char *name, void *dst);
+
+/* Names of all datasets, separated by ','. */
+const char *mpaso_genmesh_names(void);
+
+void mpaso_genmesh_free(mpaso_genmesh m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

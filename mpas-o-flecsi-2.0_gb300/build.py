@@ -1,0 +1,93 @@
+"""Builds libmpaso.so (host C++ + CUDA for sm_103a) in-tree.
+
+Usage: python mpas-o-flecsi-2.0_gb300/build.py [--force]
+
+Sources under csrc/: *.cc are compiled with g++, *.cu with nvcc for
+sm_103a only; everything is linked by nvcc into lib/libmpaso.so with the CUDA
+runtime linked statically, so the library loads on hosts without a GPU (its
+host-only entry points work there) and on the GB300 machine after a rebuild.
+"""
+import concurrent.futures as cf
+import hashlib
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "lib", "libmpaso.so")
+INC = [os.path.join(ROOT, "include"), CSRC]
+
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                  "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+
+
+def _sources():
+    srcs = sorted(f for f in os.listdir(CSRC) if f.endswith((".cc", ".cu")))
+    hdrs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hh", ".cuh")))
+    hdrs += sorted(os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include")))
+    return srcs, hdrs
+
+
+def _digest(paths, extra):
+    h = hashlib.sha1()
+    for p in paths:
+        with open(p, "rb") as f:
+            h.update(f.read())
+    h.update(" ".join(extra).encode())
+    return h.hexdigest()
+
+
+def _compile(src, hdr_digest, verbose):
+    path = os.path.join(CSRC, src)
+    obj = os.path.join(OBJ, src + ".o")
+    stamp = obj + ".sha1"
+    flags = NVFLAGS if src.endswith(".cu") else CXXFLAGS
+    d = _digest([path], flags + [hdr_digest])
+    if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == d:
+        return obj, False
+    if src.endswith(".cu"):
+        cmd = [NVCC] + flags + [f"-I{i}" for i in INC] + ["-c", path, "-o", obj]
+    else:
+        cmd = ["g++"] + flags + [f"-I{i}" for i in INC] + ["-c", path, "-o", obj]
+    if verbose:
+        print(" ".join(cmd))
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {src}\n{r.stdout}\n{r.stderr}")
+    if verbose and r.stderr.strip():
+        print(r.stderr)
+    with open(stamp, "w") as f:
+        f.write(d)
+    return obj, True
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    srcs, hdrs = _sources()
+    hdr_digest = _digest(hdrs, [])
+    if force:
+        for f in os.listdir(OBJ):
+            os.remove(os.path.join(OBJ, f))
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        results = list(ex.map(lambda s: _compile(s, hdr_digest, verbose), srcs))
+    objs = [o for o, _ in results]
+    changed = any(c for _, c in results) or not os.path.exists(LIB)
+    if changed:
+        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread"]
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,91 @@
+"""TEST INFRASTRUCTURE ONLY: builds the CPU oracle libraries.
+
+- oracle/_build/liboracle.so: the plain-C restatement (oracle.c + sw_extra.c).
+  Builds anywhere (also on the GPU host, where it is the CPU baseline).
+- oracle/_ref/libref_L<L>_T<T>.so: the reference's own task sources compiled
+  unmodified, where they lie under the reference checkout, against the header
+  shim in oracle/shim/, plus ref_driver.cc.  Built only when the reference
+  checkout is present (MPASO_REFERENCE_DIR, default /root/reference); the
+  outputs are git-ignored.
+
+Usage: python oracle/build.py [--force]
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("MPASO_REFERENCE_DIR", "/root/reference")
+CFLAGS = ["-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
+REF_SOURCES = ["apps/sw/tasks/solve.cc", "apps/ocean/tasks/solve.cc",
+               "apps/ocean/tasks/init_functions.cc"]
+# (levels, tracers) of the reference builds used by the pin tests.
+REF_CONFIGS = [(1, 1), (3, 2), (5, 5)]
+GRAVITY = "9.80616"  # mpasoflecsi/common/constants.hh:370-371
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
+
+
+def _stale(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_restatement(force=False):
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "liboracle.so")
+    deps = [os.path.join(HERE, f) for f in ("oracle.c", "sw_extra.c", "oracle.h", "build.py")]
+    if force or _stale(out, deps):
+        _run(["gcc", "-std=c11", *CFLAGS, "-shared", "-o", out, deps[0], deps[1], "-lm"])
+    return out
+
+
+def ref_available():
+    return all(os.path.exists(os.path.join(REF, s)) for s in REF_SOURCES)
+
+
+def build_ref(force=False):
+    """Returns {(L, T): path} for the reference builds (empty if no checkout)."""
+    if not ref_available():
+        return {}
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    shim = os.path.join(HERE, "shim")
+    shim_deps = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs]
+    deps = shim_deps + [os.path.join(HERE, f) for f in ("ref_driver.cc", "sw_extra.c", "oracle.h", "build.py")]
+
+    def one(cfg):
+        L, T = cfg
+        out = os.path.join(out_dir, f"libref_L{L}_T{T}.so")
+        if not (force or _stale(out, deps)):
+            return cfg, out
+        defs = [f"-DMPASO_REF_NVL={L}", f"-DMPASO_REF_NTR={T}", f"-DMPASO_REF_GRAVITY={GRAVITY}"]
+        objs = []
+        for src in REF_SOURCES + ["ref_driver.cc"]:
+            path = os.path.join(REF, src) if src in REF_SOURCES else os.path.join(HERE, src)
+            obj = os.path.join(out_dir, f"L{L}_T{T}_" + src.replace("/", "_") + ".o")
+            _run(["g++", "-std=c++17", *CFLAGS, *defs, f"-I{shim}", f"-I{REF}", f"-I{HERE}",
+                  "-w", "-c", path, "-o", obj])
+            objs.append(obj)
+        obj = os.path.join(out_dir, f"L{L}_T{T}_sw_extra.o")
+        _run(["gcc", "-std=c11", *CFLAGS, f"-I{HERE}", "-c", os.path.join(HERE, "sw_extra.c"), "-o", obj])
+        objs.append(obj)
+        _run(["g++", "-shared", "-o", out, *objs, "-lm"])
+        return cfg, out
+
+    with ThreadPoolExecutor(max_workers=len(REF_CONFIGS)) as ex:
+        return dict(ex.map(one, REF_CONFIGS))
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_restatement(force))
+    print(build_ref(force))

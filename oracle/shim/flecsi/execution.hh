@@ -1,0 +1,26 @@
+// Oracle shim (test infrastructure only): program_option stand-in.  The
+// drivers set option values directly (the reference reads them from the CLI).
+#pragma once
+#include <initializer_list>
+#include <utility>
+
+#include "flecsi/data.hh"
+
+namespace flecsi {
+
+struct option_default_t {};
+inline constexpr option_default_t option_default{};
+
+template <class T> struct program_option {
+  T v{};
+  program_option(const char *, const char *, int) {}
+  program_option(const char *, const char *, const char *,
+                 std::initializer_list<std::pair<option_default_t, T>> init) {
+    for (auto &p : init) v = p.second;
+  }
+  T value() const { return v; }
+  void set(T x) { v = x; }
+  friend bool operator==(const program_option &o, const T &x) { return o.v == x; }
+};
+
+}  // namespace flecsi
