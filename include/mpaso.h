@@ -1,0 +1,209 @@
+/*
+ * mpaso.h -- C ABI of libmpaso's GB300 (sm_103a) path for MPAS-O-FleCSI's
+ * RK4 tendency tasks.
+ *
+ * Drop-in boundary: the reference launches its tasks through FleCSI,
+ *   flecsi::execute<task::compute_tend>(m, areaCell(m), ...)  (apps/sw/run.cc:15-69,
+ *   apps/ocean/run.cc:12-48),
+ * with field accessors over per-entity AoS storage (mpasoflecsi/common/types.hh:31-46).
+ * Each per-task entry below takes the same fields, in the same order and the
+ * same AoS layouts, as raw pointers (host or device memory, detected per
+ * pointer) in the reference's entity numbering.  Static mesh fields
+ * (areaCell, dvEdge, dcEdge, weightsOnEdge, ...) are given once, at mesh
+ * context creation; a task wrapper with the reference's signature passes the
+ * per-step fields and ignores the static accessors.
+ *
+ * Internally the mesh is renumbered along a Hilbert curve (an exact integer
+ * permutation, see mpaso_mesh_permutation), fields live in HBM in that order,
+ * and every kernel gathers over precomputed connectivity without atomics.
+ *
+ * Conventions:
+ *   - every call returns MPASO_OK (0) or an MPASO_ERR_* code (mpaso_mesh.h);
+ *     mpaso_last_error() gives the calling thread's message; no exception
+ *     crosses the ABI;
+ *   - a context is used by one host thread at a time; distinct contexts may be
+ *     used concurrently;
+ *   - `stream` is a cudaStream_t (NULL = the context's own stream).  Calls
+ *     with any host pointer are synchronous; calls with only device pointers
+ *     are asynchronous on the stream.
+ */
+#ifndef MPASO_H
+#define MPASO_H
+
+#include <stdint.h>
+
+#include "mpaso_mesh.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mpaso_mesh_s *mpaso_mesh;
+typedef struct mpaso_state_s *mpaso_state;
+
+/* Mesh description in the reference's terms.  Connectivity is FleCSI's CRS
+ * (0-based) in file order: c2v = verticesOnCell, c2e = edgesOnCell,
+ * c2c = cellsOnCell, e2v = verticesOnEdge, e2e = edgesOnEdge
+ * (mpasoflecsi/specialization/mesh.cc:221-243).  The transposes v2c, e2c, v2e
+ * are built inside, as mesh.cc:262-270 builds them (ascending ids). */
+typedef struct {
+  int64_t nCells, nEdges, nVertices;
+  const int64_t *c2v_off, *c2e_off, *c2c_off, *e2v_off, *e2e_off;
+  const int32_t *c2v, *c2e, *c2c, *e2v, *e2e;
+  /* geometry (mpasoflecsi/specialization/mesh.hh:114-152) */
+  const double *areaCell, *dvEdge, *dcEdge, *areaTriangle;
+  const double *kiteAreasOnVertex; /* [nV][3] */
+  const double *fVertex;
+  const double *weightsOnEdge; /* [nE][16] */
+  const double *bottomDepth;   /* h_s of the sw app; NULL = 0 */
+  /* cell centres: used only to build the Hilbert ordering; NULL = keep order */
+  const double *xCell, *yCell, *zCell;
+  int32_t reorder; /* 1 = renumber along a Hilbert curve, 0 = keep numbering */
+  /* FCT / del2 statics (apps/ocean/state.hh:261-294); NULL = not available */
+  int32_t fct_nlev; /* level count of highOrderAdvMask */
+  const int32_t *maxLevelCell, *maxLevelEdgeTop, *nAdvCellsForEdge;
+  const int32_t *advCellsForEdge;  /* [nE][16] */
+  const int32_t *highOrderAdvMask; /* [nE][fct_nlev] */
+  const double *edgeSignOnCell;    /* [nC][8] */
+  const double *advCoef, *advCoef_3rd; /* [nE][16] */
+  const double *meshScalingDel2;
+} mpaso_mesh_desc;
+
+#define MPASO_CELLS 0
+#define MPASO_EDGES 1
+#define MPASO_VERTICES 2
+
+/* Builds the device mesh context on `device` (-1 = current device). */
+int mpaso_mesh_create(const mpaso_mesh_desc *desc, int device, mpaso_mesh *out);
+int mpaso_mesh_destroy(mpaso_mesh m);
+/* new_to_old[new] = reference id, for MPASO_CELLS/EDGES/VERTICES. */
+int mpaso_mesh_permutation(mpaso_mesh m, int32_t entity, int32_t *new_to_old);
+/* Gravity used by compute_tend (the reference's mpas_constants::gravity,
+ * mpasoflecsi/common/constants.hh:370-371; default 9.80616). */
+int mpaso_mesh_set_gravity(mpaso_mesh m, double gravity);
+/* Bytes of device memory held by the context. */
+int mpaso_mesh_device_bytes(mpaso_mesh m, int64_t *bytes);
+
+/* ------------------------------------------------------------------------
+ * Per-task entries, one per reference task.  Arrays: vlreal [n][L],
+ * vltracer [n][L][T], in the reference's numbering.  nlev / ntr are the
+ * reference's nVertLevels / maxTracers (compile-time there).
+ * ---------------------------------------------------------------------- */
+
+/* apps/sw/tasks/solve.cc:11-107 */
+int mpaso_sw_compute_solve_diagnostics(mpaso_mesh m, int32_t nlev, const double *h,
+                                       const double *u, double *h_edge, double *h_vertex,
+                                       double *circulation, double *vorticity, double *ke,
+                                       double *pv_edge, double *pv_vertex, void *stream);
+/* apps/sw/tasks/solve.cc:169-234 */
+int mpaso_sw_compute_tend(mpaso_mesh m, int32_t nlev, const double *h_edge, const double *h,
+                          const double *u, const double *ke, const double *pv_edge,
+                          double *tend_h, double *tend_u, void *stream);
+/* apps/sw/tasks/solve.cc:237-270 */
+int mpaso_sw_compute_scalar_tend(mpaso_mesh m, int32_t nlev, int32_t ntr, const double *h_edge,
+                                 const double *u, const double *tracers, double *tracer_tend,
+                                 void *stream);
+/* apps/sw/tasks/solve.cc:273-314; pin_u = 1 reproduces test case 1 */
+int mpaso_sw_compute_substep(mpaso_mesh m, int32_t nlev, int32_t ntr, double *u_provis,
+                             const double *u_old, const double *u_tend, double *h_provis,
+                             const double *h_old, const double *h_tend, double *tracers_provis,
+                             const double *tracers_old, const double *tracers_tend,
+                             double rkweight, int32_t pin_u, void *stream);
+/* apps/sw/tasks/solve.cc:317-341 */
+int mpaso_sw_accumulate_update(mpaso_mesh m, int32_t nlev, int32_t ntr, double *u_new,
+                               const double *u_tend, double *h_new, const double *h_tend,
+                               double *tracers_new, const double *tracers_tend, double rkweight,
+                               void *stream);
+/* apps/sw/tasks/solve.cc:344-367 */
+int mpaso_sw_finalize_timestep(mpaso_mesh m, int32_t nlev, int32_t ntr, const double *u_old,
+                               double *u_new, const double *h_new, double *tracers_new,
+                               int32_t pin_u, void *stream);
+
+/* apps/ocean/tasks/solve.cc:40-57 */
+int mpaso_oc_calc_normal_thickness_flux(mpaso_mesh m, int32_t nlev,
+                                        const double *layerThicknessEdge,
+                                        const double *normalVelocity,
+                                        double *normalThicknessFlux, void *stream);
+/* apps/ocean/tasks/solve.cc:60-97 (w is unused, as in the reference) */
+int mpaso_oc_calc_provisional_layer_thicknesses(mpaso_mesh m, int32_t nlev,
+                                                const double *layerThickness,
+                                                const double *normalThicknessFlux,
+                                                double *hProv, double *hProvInv, double *hNewInv,
+                                                double dt, void *stream);
+/* apps/ocean/tasks/solve.cc:99-118 */
+int mpaso_oc_calc_horiz_tracer_advection_flux_mono_low_order(
+    mpaso_mesh m, int32_t nlev, int32_t ntr, const double *normalThicknessFlux,
+    const double *tracers, double *lowOrderFlux, void *stream);
+/* apps/ocean/tasks/solve.cc:120-167 */
+int mpaso_oc_calc_horiz_tracer_advection_flux_mono_high_order(
+    mpaso_mesh m, int32_t nlev, int32_t ntr, const double *normalThicknessFlux,
+    const double *tracers, double *highOrderFlux, void *stream);
+/* apps/ocean/tasks/solve.cc:169-285 */
+int mpaso_oc_correct_and_rescale_high_order_mono_horiz_flux(
+    mpaso_mesh m, int32_t nlev, int32_t ntr, const double *hProvInv, const double *layerThickness,
+    const double *normalThicknessFlux, const double *lowOrderFlux, const double *tracers,
+    double *highOrderFlux, double *flxIn, double *flxOut, double *tend, double *tracerMax,
+    double *tracerMin, double dt, void *stream);
+/* apps/ocean/tasks/solve.cc:287-326 */
+int mpaso_oc_accumulate_horiz_tracer_advection_tend_mono_FCT(
+    mpaso_mesh m, int32_t nlev, int32_t ntr, const double *hProvInv, const double *layerThickness,
+    const double *highOrderFlux, const double *tracers, double *tracersProv, double *tend,
+    double dt, void *stream);
+/* apps/ocean/tasks/solve.cc:328-366 */
+int mpaso_oc_tracer_hmix_del2_tend(mpaso_mesh m, int32_t nlev, int32_t ntr,
+                                   const double *layerThicknessEdge, const double *tracers,
+                                   double *tend, double coef, void *stream);
+/* apps/ocean/tasks/solve.cc:368-399 */
+int mpaso_oc_step_tracers_forward(mpaso_mesh m, int32_t nlev, int32_t ntr, const double *tend,
+                                  const double *tracers, double *tracersNew, double *tracersPrev,
+                                  double rk_weight, double rk_subweight, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Fused RK4 path: state resident in HBM, one call advances nsteps.
+ * ---------------------------------------------------------------------- */
+#define MPASO_APP_SW 0    /* apps/sw/run.cc:13-70 (+ FCT tracer coupling) */
+#define MPASO_APP_OCEAN 1 /* apps/ocean/run.cc:10-50 */
+
+typedef struct {
+  int32_t app;
+  int32_t nlev, ntr;
+  double gravity; /* sw */
+  int32_t fct;    /* FCT tracer advection (sw: replaces compute_scalar_tend) */
+  int32_t hmix;   /* del2 tracer mixing */
+  double kappa;   /* del2 tracer coefficient, m^2/s */
+  double nu;      /* del2 momentum viscosity, m^2/s (sw; not in the reference) */
+  int32_t pin_u;  /* sw test case 1 */
+} mpaso_params;
+
+#define MPASO_FIELD_H 0                    /* sw h / ocean layerThickness [nC][L] */
+#define MPASO_FIELD_U 1                    /* sw u / ocean normalVelocity [nE][L] */
+#define MPASO_FIELD_TRACERS 2              /* [nC][L][T] */
+#define MPASO_FIELD_LAYER_THICKNESS_EDGE 3 /* ocean layerThicknessEdge [nE][L] */
+
+int mpaso_state_create(mpaso_mesh m, const mpaso_params *p, mpaso_state *out);
+int mpaso_state_destroy(mpaso_state s);
+/* Copy a field in (reference numbering, host or device memory). */
+int mpaso_state_set(mpaso_state s, int32_t field, const double *data);
+/* Copy a field out (reference numbering, host or device memory). */
+int mpaso_state_get(mpaso_state s, int32_t field, double *data);
+/* Advance nsteps RK4 steps of size dt; asynchronous on the state's stream. */
+int mpaso_rk4_step(mpaso_state s, double dt, int32_t nsteps);
+/* Same, replayed from a CUDA graph of one step (captured on first use for dt). */
+int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps);
+/* One call through the boundary with host buffers: copy in, nsteps, copy out. */
+int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                        double *tracers);
+int mpaso_state_sync(mpaso_state s);
+int mpaso_state_stream(mpaso_state s, void **stream);
+/* Kernel launches issued per RK4 step by mpaso_rk4_step. */
+int mpaso_state_launches_per_step(mpaso_state s, int32_t *n);
+int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
+
+/* Device / runtime queries (no GPU needed: report 0 devices). */
+int mpaso_device_count(int32_t *n);
+const char *mpaso_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,388 @@
+// Mesh context: builds the device-resident mesh from the reference's
+// connectivity (mpasoflecsi/specialization/mesh.cc:221-270 semantics),
+// renumbers it along a Hilbert curve, and uploads slot-major arrays to HBM.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "device.cuh"
+
+namespace mpaso {
+
+MeshCtx::~MeshCtx() {
+  if (arena) cudaFree(arena);
+  if (scratch) cudaFree(scratch);
+  for (auto &p : d_perm)
+    if (p) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void *MeshCtx::ensure_scratch(size_t bytes) {
+  if (bytes <= scratch_bytes) return scratch;
+  if (scratch) {
+    MPASO_CUDA(cudaStreamSynchronize(stream));
+    MPASO_CUDA(cudaFree(scratch));
+    scratch = nullptr;
+    scratch_bytes = 0;
+  }
+  const size_t want = std::max(bytes, scratch_bytes * 3 / 2);
+  if (cudaMalloc(&scratch, want) != cudaSuccess) {
+    cudaGetLastError();
+    fail(MPASO_ERR_ALLOC, "device scratch allocation of " + std::to_string(want) + " bytes failed");
+  }
+  scratch_bytes = want;
+  return scratch;
+}
+
+namespace {
+
+struct Crs {
+  std::vector<int64_t> off;
+  std::vector<int32_t> idx;
+  int64_t n() const { return (int64_t)off.size() - 1; }
+  int64_t len(int64_t i) const { return off[i + 1] - off[i]; }
+  int32_t at(int64_t i, int64_t j) const { return idx[off[i] + j]; }
+};
+
+Crs copy_crs(const int64_t *off, const int32_t *idx, int64_t n, int64_t n_to, const char *name) {
+  require(off && idx, MPASO_ERR_ARG, std::string("missing connectivity ") + name);
+  Crs c;
+  c.off.assign(off, off + n + 1);
+  require(c.off[0] == 0, MPASO_ERR_MESH, std::string(name) + ": offsets must start at 0");
+  for (int64_t i = 0; i < n; ++i)
+    require(c.off[i + 1] >= c.off[i], MPASO_ERR_MESH, std::string(name) + ": offsets decrease");
+  c.idx.assign(idx, idx + c.off[n]);
+  for (int32_t v : c.idx)
+    require(v >= 0 && v < n_to, MPASO_ERR_MESH, std::string(name) + ": index out of range");
+  return c;
+}
+
+// v2c[c2v[c][v]].push_back(c) -- mpasoflecsi/specialization/mesh.cc:262-270.
+Crs transpose(const Crs &a, int64_t n_to) {
+  Crs t;
+  t.off.assign(n_to + 1, 0);
+  for (int32_t v : a.idx) t.off[v + 1]++;
+  for (int64_t i = 0; i < n_to; ++i) t.off[i + 1] += t.off[i];
+  t.idx.resize(a.idx.size());
+  std::vector<int64_t> fill(t.off.begin(), t.off.end() - 1);
+  for (int64_t i = 0; i < a.n(); ++i)
+    for (int64_t j = a.off[i]; j < a.off[i + 1]; ++j) t.idx[fill[a.idx[j]]++] = (int32_t)i;
+  return t;
+}
+
+// Device arena: sub-allocations aligned to 256 B inside one cudaMalloc.
+struct Arena {
+  struct Item {
+    const void *src;
+    size_t bytes;
+    size_t off;
+    const void **dst;
+  };
+  std::vector<Item> items;
+  std::vector<std::vector<char>> owned;
+  size_t total = 0;
+  template <class T> void add(const std::vector<T> &v, const T **dst) {
+    owned.emplace_back((const char *)v.data(), (const char *)v.data() + v.size() * sizeof(T));
+    items.push_back({owned.back().data(), v.size() * sizeof(T), total, (const void **)dst});
+    total += (v.size() * sizeof(T) + 255) & ~size_t(255);
+  }
+  void upload(MeshCtx &ctx) {
+    if (cudaMalloc(&ctx.arena, std::max<size_t>(total, 256)) != cudaSuccess) {
+      cudaGetLastError();
+      fail(MPASO_ERR_ALLOC, "device allocation of the mesh context failed");
+    }
+    ctx.arena_bytes = total;
+    std::vector<char> host(total, 0);
+    for (auto &it : items) std::memcpy(host.data() + it.off, it.src, it.bytes);
+    MPASO_CUDA(cudaMemcpy(ctx.arena, host.data(), total, cudaMemcpyHostToDevice));
+    for (auto &it : items) *it.dst = (const char *)ctx.arena + it.off;
+  }
+};
+
+void build(MeshCtx &ctx, const mpaso_mesh_desc &d) {
+  const int64_t nC = d.nCells, nE = d.nEdges, nV = d.nVertices;
+  require(nC > 0 && nE > 0 && nV > 0 && nE < (1LL << 30), MPASO_ERR_ARG, "bad entity counts");
+  require(d.areaCell && d.dvEdge && d.dcEdge && d.areaTriangle && d.kiteAreasOnVertex && d.fVertex &&
+              d.weightsOnEdge,
+          MPASO_ERR_ARG, "missing geometry field");
+  const Crs c2v = copy_crs(d.c2v_off, d.c2v, nC, nV, "c2v");
+  const Crs c2e = copy_crs(d.c2e_off, d.c2e, nC, nE, "c2e");
+  const Crs c2c = copy_crs(d.c2c_off, d.c2c, nC, nC, "c2c");
+  const Crs e2v = copy_crs(d.e2v_off, d.e2v, nE, nV, "e2v");
+  const Crs e2e = copy_crs(d.e2e_off, d.e2e, nE, nE, "e2e");
+  const Crs v2c = transpose(c2v, nV), e2c = transpose(c2e, nE), v2e = transpose(e2v, nV);
+  for (int64_t e = 0; e < nE; ++e) {
+    require(e2c.len(e) == 2, MPASO_ERR_MESH, "every edge needs exactly two cells");
+    require(e2v.len(e) == 2, MPASO_ERR_MESH, "every edge needs exactly two vertices");
+    require(e2e.len(e) <= kMaxEdges2, MPASO_ERR_MESH, "edgesOnEdge longer than maxEdges2");
+  }
+  for (int64_t v = 0; v < nV; ++v) {
+    require(v2c.len(v) == kVertexDegree, MPASO_ERR_MESH, "every vertex needs three cells");
+    require(v2e.len(v) == kVertexDegree, MPASO_ERR_MESH, "every vertex needs three edges");
+  }
+  int maxEoC = 0, maxEoE = 0;
+  for (int64_t c = 0; c < nC; ++c) {
+    require(c2e.len(c) <= kMaxEdges && c2e.len(c) >= 1, MPASO_ERR_MESH, "edgesOnCell length");
+    require(c2c.len(c) == c2e.len(c), MPASO_ERR_MESH, "cellsOnCell / edgesOnCell length mismatch");
+    maxEoC = std::max(maxEoC, (int)c2e.len(c));
+  }
+  for (int64_t e = 0; e < nE; ++e) maxEoE = std::max(maxEoE, (int)e2e.len(e));
+
+  // ---- permutation ----
+  std::vector<int32_t> pc(nC), pe(nE), pv(nV);
+  std::iota(pc.begin(), pc.end(), 0);
+  if (d.reorder) {
+    require(d.xCell && d.yCell, MPASO_ERR_ARG, "reorder needs xCell/yCell(/zCell)");
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    const double *xyz[3] = {d.xCell, d.yCell, d.zCell};
+    const int dims = d.zCell ? 3 : 2;
+    for (int a = 0; a < dims; ++a)
+      for (int64_t c = 0; c < nC; ++c) lo[a] = std::min(lo[a], xyz[a][c]), hi[a] = std::max(hi[a], xyz[a][c]);
+    const int bits = dims == 3 ? 20 : 30;
+    std::vector<uint64_t> key(nC);
+    for (int64_t c = 0; c < nC; ++c) {
+      uint32_t q[3] = {0, 0, 0};
+      for (int a = 0; a < dims; ++a) {
+        const double span = hi[a] > lo[a] ? hi[a] - lo[a] : 1.0;
+        q[a] = (uint32_t)((xyz[a][c] - lo[a]) / span * (double)((1u << bits) - 1));
+      }
+      key[c] = hilbert_key(q, dims, bits);
+    }
+    std::stable_sort(pc.begin(), pc.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  }
+  std::vector<int32_t> ic(nC);
+  for (int64_t k = 0; k < nC; ++k) ic[pc[k]] = (int32_t)k;
+  std::iota(pe.begin(), pe.end(), 0);
+  std::iota(pv.begin(), pv.end(), 0);
+  if (d.reorder) {
+    auto ekey = [&](int32_t e) {
+      const int32_t a = ic[e2c.at(e, 0)], b = ic[e2c.at(e, 1)];
+      return std::make_pair(std::min(a, b), std::max(a, b));
+    };
+    std::stable_sort(pe.begin(), pe.end(), [&](int32_t a, int32_t b) { return ekey(a) < ekey(b); });
+    auto vkey = [&](int32_t v) {
+      int32_t m = INT32_MAX;
+      for (int j = 0; j < kVertexDegree; ++j) m = std::min(m, ic[v2c.at(v, j)]);
+      return m;
+    };
+    std::stable_sort(pv.begin(), pv.end(), [&](int32_t a, int32_t b) { return vkey(a) < vkey(b); });
+  }
+  std::vector<int32_t> ie(nE), iv(nV);
+  for (int64_t k = 0; k < nE; ++k) ie[pe[k]] = (int32_t)k;
+  for (int64_t k = 0; k < nV; ++k) iv[pv[k]] = (int32_t)k;
+
+  // ---- cells ----
+  Arena A;
+  DMesh &m = ctx.d;
+  m.nC = (int)nC, m.nE = (int)nE, m.nV = (int)nV, m.maxEoC = maxEoC, m.maxEoE = maxEoE;
+  std::vector<int> nEoC(nC), eoc((size_t)maxEoC * nC), eocAsc((size_t)maxEoC * nC), coc((size_t)maxEoC * nC);
+  std::vector<double> eocSign((size_t)maxEoC * nC, 0.0), eocAscSign((size_t)maxEoC * nC, 0.0);
+  std::vector<double> area(nC), invArea(nC), hs(nC, 0.0);
+  std::vector<int> mlc(nC, 1);
+  const Crs c2eAsc = transpose(e2c, nC);  // edges of each cell, ascending reference id
+  for (int64_t k = 0; k < nC; ++k) {
+    const int32_t c = pc[k];
+    const int n = (int)c2e.len(c);
+    nEoC[k] = n;
+    for (int j = 0; j < maxEoC; ++j) {
+      const size_t s = (size_t)j * nC + k;
+      if (j < n) {
+        const int32_t e = c2e.at(c, j);
+        eoc[s] = ie[e];
+        coc[s] = ic[c2c.at(c, j)];
+        eocSign[s] = d.edgeSignOnCell ? d.edgeSignOnCell[(size_t)c * kMaxEdges + j]
+                                      : (c == e2c.at(e, 0) ? -1.0 : 1.0);
+        const int32_t ea = c2eAsc.at(c, j);
+        eocAsc[s] = ie[ea];
+        eocAscSign[s] = (c == e2c.at(ea, 0)) ? -1.0 : 1.0;
+      } else {  // pad: repeat slot 0 with a zero sign
+        eoc[s] = ie[c2e.at(c, 0)];
+        coc[s] = k;
+        eocAsc[s] = ie[c2e.at(c, 0)];
+      }
+    }
+    area[k] = d.areaCell[c];
+    invArea[k] = 1.0 / d.areaCell[c];
+    if (d.bottomDepth) hs[k] = d.bottomDepth[c];
+    if (d.maxLevelCell) mlc[k] = d.maxLevelCell[c];
+  }
+  A.add(nEoC, &m.nEoC), A.add(eoc, &m.eoc), A.add(eocSign, &m.eocSign), A.add(eocAsc, &m.eocAsc);
+  A.add(eocAscSign, &m.eocAscSign), A.add(coc, &m.coc), A.add(area, &m.areaCell);
+  A.add(invArea, &m.invAreaCell), A.add(hs, &m.bottomDepth), A.add(mlc, &m.maxLevelCell);
+
+  // ---- edges ----
+  std::vector<int2> coe(nE), voe(nE);
+  std::vector<double> dv(nE), dc(nE), idc(nE), idv(nE), msd(nE, 1.0);
+  std::vector<int> nEoE(nE), eoe((size_t)std::max(maxEoE, 1) * nE), mlet(nE, 1);
+  std::vector<double> woe((size_t)std::max(maxEoE, 1) * nE, 0.0);
+  for (int64_t k = 0; k < nE; ++k) {
+    const int32_t e = pe[k];
+    coe[k] = make_int2(ic[e2c.at(e, 0)], ic[e2c.at(e, 1)]);
+    voe[k] = make_int2(iv[e2v.at(e, 0)], iv[e2v.at(e, 1)]);
+    dv[k] = d.dvEdge[e], dc[k] = d.dcEdge[e];
+    idc[k] = 1.0 / d.dcEdge[e], idv[k] = 1.0 / d.dvEdge[e];
+    const int n = (int)e2e.len(e);
+    nEoE[k] = n;
+    for (int j = 0; j < maxEoE; ++j) {
+      const size_t s = (size_t)j * nE + k;
+      if (j < n) {
+        eoe[s] = ie[e2e.at(e, j)];
+        woe[s] = d.weightsOnEdge[(size_t)e * kMaxEdges2 + j];
+      } else {
+        eoe[s] = (int)k;  // pad: own edge with zero weight
+      }
+    }
+    if (d.maxLevelEdgeTop) mlet[k] = d.maxLevelEdgeTop[e];
+    if (d.meshScalingDel2) msd[k] = d.meshScalingDel2[e];
+  }
+  A.add(coe, &m.coe), A.add(voe, &m.voe), A.add(dv, &m.dvEdge), A.add(dc, &m.dcEdge);
+  A.add(idc, &m.invDcEdge), A.add(idv, &m.invDvEdge), A.add(nEoE, &m.nEoE), A.add(eoe, &m.eoe);
+  A.add(woe, &m.woe), A.add(mlet, &m.maxLevelEdgeTop), A.add(msd, &m.meshScalingDel2);
+
+  // ---- FCT statics ----
+  ctx.has_fct = d.nAdvCellsForEdge && d.advCellsForEdge && d.advCoef && d.advCoef_3rd &&
+                d.highOrderAdvMask && d.fct_nlev > 0;
+  int maxAdv = 1;
+  if (ctx.has_fct)
+    for (int64_t e = 0; e < nE; ++e) {
+      require(d.nAdvCellsForEdge[e] >= 0 && d.nAdvCellsForEdge[e] <= kMaxEdges2, MPASO_ERR_MESH,
+              "nAdvCellsForEdge out of range");
+      maxAdv = std::max(maxAdv, (int)d.nAdvCellsForEdge[e]);
+    }
+  m.maxAdv = maxAdv;
+  m.fctLev = ctx.has_fct ? d.fct_nlev : 1;
+  std::vector<int> nAdv(nE, 0), advCells((size_t)maxAdv * nE, 0), mask((size_t)nE * m.fctLev, 1);
+  std::vector<double> ac((size_t)maxAdv * nE, 0.0), a3((size_t)maxAdv * nE, 0.0);
+  std::vector<double> cp((size_t)maxAdv * nE, 0.0), cm((size_t)maxAdv * nE, 0.0);
+  if (ctx.has_fct) {
+    for (int64_t k = 0; k < nE; ++k) {
+      const int32_t e = pe[k];
+      const int n = d.nAdvCellsForEdge[e];
+      nAdv[k] = n;
+      for (int j = 0; j < maxAdv; ++j) {
+        const size_t s = (size_t)j * nE + k;
+        if (j < n) {
+          const int32_t cc = d.advCellsForEdge[(size_t)e * kMaxEdges2 + j];
+          require(cc >= 0 && cc < nC, MPASO_ERR_MESH, "advCellsForEdge out of range");
+          advCells[s] = ic[cc];
+          const double c1 = d.advCoef[(size_t)e * kMaxEdges2 + j];
+          const double c3 = d.advCoef_3rd[(size_t)e * kMaxEdges2 + j] * 0.25;  // coef3rdOrder
+          ac[s] = c1, a3[s] = d.advCoef_3rd[(size_t)e * kMaxEdges2 + j];
+          cp[s] = c1 + c3, cm[s] = c1 - c3;
+        } else {
+          advCells[s] = coe[k].x;
+        }
+      }
+      for (int l = 0; l < m.fctLev; ++l) mask[(size_t)k * m.fctLev + l] = d.highOrderAdvMask[(size_t)e * m.fctLev + l];
+    }
+  }
+  A.add(nAdv, &m.nAdv), A.add(advCells, &m.advCells), A.add(ac, &m.advCoef), A.add(a3, &m.advCoef3);
+  A.add(cp, &m.advCp), A.add(cm, &m.advCm), A.add(mask, &m.hoMask);
+
+  // ---- vertices ----
+  std::vector<int> cov((size_t)kVertexDegree * nV), eov((size_t)kVertexDegree * nV);
+  std::vector<double> kite((size_t)kVertexDegree * nV), eovSign((size_t)kVertexDegree * nV);
+  std::vector<double> aT(nV), iaT(nV), fV(nV);
+  for (int64_t k = 0; k < nV; ++k) {
+    const int32_t v = pv[k];
+    for (int j = 0; j < kVertexDegree; ++j) {
+      const size_t s = (size_t)j * nV + k;
+      cov[s] = ic[v2c.at(v, j)];
+      kite[s] = d.kiteAreasOnVertex[(size_t)v * kVertexDegree + j];
+      const int32_t e = v2e.at(v, j);
+      eov[s] = ie[e];
+      eovSign[s] = (e2v.at(e, 0) == v) ? -1.0 : 1.0;
+    }
+    aT[k] = d.areaTriangle[v], iaT[k] = 1.0 / d.areaTriangle[v], fV[k] = d.fVertex[v];
+  }
+  A.add(cov, &m.cov), A.add(kite, &m.kite), A.add(eov, &m.eov), A.add(eovSign, &m.eovSign);
+  A.add(aT, &m.areaTriangle), A.add(iaT, &m.invAreaTriangle), A.add(fV, &m.fVertex);
+
+  A.upload(ctx);
+  ctx.perm[0] = pc, ctx.perm[1] = pe, ctx.perm[2] = pv;
+  ctx.iperm[0] = ic, ctx.iperm[1] = ie, ctx.iperm[2] = iv;
+  for (int t = 0; t < 3; ++t) {
+    const size_t bytes = ctx.perm[t].size() * sizeof(int32_t);
+    MPASO_CUDA(cudaMalloc(&ctx.d_perm[t], bytes));
+    MPASO_CUDA(cudaMemcpy(ctx.d_perm[t], ctx.perm[t].data(), bytes, cudaMemcpyHostToDevice));
+  }
+}
+
+}  // namespace
+}  // namespace mpaso
+
+extern "C" {
+
+int mpaso_device_count(int32_t *n) {
+  return mpaso::guarded("mpaso_device_count", [&] {
+    mpaso::require(n != nullptr, MPASO_ERR_ARG, "null output");
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+      cudaGetLastError();
+      c = 0;
+    }
+    *n = c;
+  });
+}
+
+const char *mpaso_build_info(void) {
+  return "libmpaso: FP64 MPAS-O-FleCSI RK4 tendency path for sm_103a (GB300)";
+}
+
+int mpaso_mesh_create(const mpaso_mesh_desc *desc, int device, mpaso_mesh *out) {
+  return mpaso::guarded("mpaso_mesh_create", [&] {
+    mpaso::require(desc != nullptr && out != nullptr, MPASO_ERR_ARG, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      mpaso::fail(MPASO_ERR_NODEVICE, "no CUDA device");
+    }
+    if (device < 0) MPASO_CUDA(cudaGetDevice(&device));
+    mpaso::require(device < ndev, MPASO_ERR_ARG, "device index out of range");
+    MPASO_CUDA(cudaSetDevice(device));
+    auto *h = new mpaso_mesh_s();
+    try {
+      h->ctx.device = device;
+      MPASO_CUDA(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking));
+      mpaso::build(h->ctx, *desc);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int mpaso_mesh_destroy(mpaso_mesh m) {
+  return mpaso::guarded("mpaso_mesh_destroy", [&] {
+    if (!m) return;
+    cudaSetDevice(m->ctx.device);
+    cudaStreamSynchronize(m->ctx.stream);
+    delete m;
+  });
+}
+
+int mpaso_mesh_permutation(mpaso_mesh m, int32_t entity, int32_t *new_to_old) {
+  return mpaso::guarded("mpaso_mesh_permutation", [&] {
+    mpaso::require(m && new_to_old && entity >= 0 && entity < 3, MPASO_ERR_ARG, "bad argument");
+    const auto &p = m->ctx.perm[entity];
+    std::memcpy(new_to_old, p.data(), p.size() * sizeof(int32_t));
+  });
+}
+
+int mpaso_mesh_set_gravity(mpaso_mesh m, double gravity) {
+  return mpaso::guarded("mpaso_mesh_set_gravity", [&] {
+    mpaso::require(m != nullptr, MPASO_ERR_ARG, "null mesh");
+    m->ctx.gravity = gravity;
+  });
+}
+
+int mpaso_mesh_device_bytes(mpaso_mesh m, int64_t *bytes) {
+  return mpaso::guarded("mpaso_mesh_device_bytes", [&] {
+    mpaso::require(m && bytes, MPASO_ERR_ARG, "null argument");
+    *bytes = (int64_t)(m->ctx.arena_bytes + m->ctx.scratch_bytes);
+  });
+}
+
+}  // extern "C"

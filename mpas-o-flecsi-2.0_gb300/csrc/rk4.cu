@@ -1,0 +1,561 @@
+// Fused RK4 path of the sw app (apps/sw/run.cc:13-70) with the FCT tracer
+// coupling, del2 tracer mixing and del2 momentum, on the renumbered HBM layout.
+//
+// Per RK stage three launches, no copies:
+//   K1 edge pre-pass   : thickness flux F = u h_e, F pv_e, FCT low/high-order
+//                        fluxes -> anti-diffusive flux A, del2 tracer flux
+//                        (apps/ocean/tasks/solve.cc:40-167, 216-229, 328-366);
+//   K2 edges + cells   : tend_u from edgesOnEdge x weightsOnEdge, KE and
+//                        geopotential gradient (apps/sw/tasks/solve.cc:215-233),
+//                        u update; tend_h (solve.cc:185-206), h update, FCT
+//                        bounds and limiter factors (ocean solve.cc:194-267);
+//   K3 cells + vertices: limited fluxes -> tracer tendency (ocean solve.cc:
+//                        269-326), thickness-weighted tracer update
+//                        (sw solve.cc:273-367), then the diagnostics of the next
+//                        stage's state (sw solve.cc:11-107).
+// The state rotates through four buffers per field, so the step needs no
+// init_provis / setup_timestep / timeshift copies.
+//
+// GB300 executes FP64 at ~1/64 of its FP32 rate, so these kernels are bound by
+// FP64 issue: multiplications by +-1 are sign-bit flips, min/max/clamp/
+// upwind selection are integer operations on the bit patterns, divisions by
+// static quantities use precomputed reciprocals, and the dynamic ones use
+// rcp_nr.  Results match the reference task sequence to rounding (about 1e-15
+// relative per step), not bit for bit.
+#include <cstring>
+
+#include "rk4.cuh"
+
+namespace mpaso {
+namespace {
+
+constexpr int TPB = 256;
+// ------------------------------------------------------------- K1: edges
+template <int T>
+__global__ void __launch_bounds__(TPB) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nE * L) return;
+  const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
+  const int2 c = m.coe[e];
+  const int2 v = m.voe[e];
+  const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
+  const double he = 0.5 * (S.h_in[i1] + S.h_in[i2]);
+  const double F = S.u_in[i] * he;
+  const double pve = 0.5 * (S.pv[(int64_t)v.x * L + k] + S.pv[(int64_t)v.y * L + k]);
+  S.F[i] = F;
+  S.G[i] = F * pve;
+  S.pve[i] = pve;
+  if constexpr (T > 0) edge_tracer_fluxes<T>(m, st, S, L, e, k, i, i1, i2, F, he);
+}
+
+// ------------------------------------------------------ K2: edges + cells
+template <int T>
+__global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nEL = (int64_t)m.nE * L;
+  if (i < nEL) {
+    const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
+    double s1 = 0.0, s2 = 0.0;
+    for (int j = 0; j < m.maxEoE; ++j) {
+      const int eo = m.eoe[(int64_t)j * m.nE + e];
+      const double w = m.woe[(int64_t)j * m.nE + e];
+      const int64_t io = (int64_t)eo * L + k;
+      s1 = fma(w, S.F[io], s1);
+      s2 = fma(w, S.G[io], s2);
+    }
+    const double q = 0.5 * fma(S.pve[i], s1, s2);
+    const int2 c = m.coe[e];
+    const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
+    const double dh = (S.h_in[i2] - S.h_in[i1]) + st.dhs[e];
+    double tend = q - fma(S.g, dh, S.ke[i2] - S.ke[i1]) * m.invDcEdge[e];
+    if (S.visc) {
+      const int2 v = m.voe[e];
+      const double dd = (S.divc[i2] - S.divc[i1]) * m.invDcEdge[e];
+      const double dz = (S.vort[(int64_t)v.y * L + k] - S.vort[(int64_t)v.x * L + k]) * m.invDvEdge[e];
+      tend = fma(S.nu, dd - dz, tend);
+    }
+    const double up = S.u_prev[i];
+    switch (S.stage) {
+      case 0:
+        S.u_out[i] = S.pin_u ? up : fma(S.w_sub, tend, up);
+        S.u_acc[i] = fma(S.w_acc, tend, up);
+        break;
+      case 3:
+        S.u_new[i] = S.pin_u ? up : fma(S.w_acc, tend, S.u_acc[i]);
+        break;
+      default:
+        S.u_out[i] = S.pin_u ? up : fma(S.w_sub, tend, up);
+        S.u_acc[i] = fma(S.w_acc, tend, S.u_acc[i]);
+    }
+    return;
+  }
+  i -= nEL;
+  if (i >= (int64_t)m.nC * L) return;
+  const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+  const int n = m.nEoC[c];
+  const double inva = m.invAreaCell[c];
+  double acc = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.eoc[(int64_t)j * m.nC + c];
+    acc = fma(st.sdv[(int64_t)j * m.nC + c], S.F[(int64_t)e * L + k], acc);
+  }
+  const double tend_h = acc * inva;
+  const double hp = S.h_prev[i];
+  switch (S.stage) {
+    case 0:
+      S.h_out[i] = fma(S.w_sub, tend_h, hp);
+      S.h_acc[i] = fma(S.w_acc, tend_h, hp);
+      break;
+    case 3:
+      S.h_new[i] = fma(S.w_acc, tend_h, S.h_acc[i]);
+      break;
+    default:
+      S.h_out[i] = fma(S.w_sub, tend_h, hp);
+      S.h_acc[i] = fma(S.w_acc, tend_h, S.h_acc[i]);
+  }
+  if constexpr (T > 0) {
+    // provisional thickness (apps/ocean/tasks/solve.cc:60-97): h + dt tend_h
+    const double hin = S.h_in[i];
+    const double hpi = S.fct ? rcp_nr(fma(S.dt, tend_h, hin)) : 0.0;
+    cell_limiter<T>(m, S, L, c, k, i, hin, hpi);
+  }
+}
+
+// Diagnostics of a state (u, h): ke, div at cells; vorticity, pv at vertices.
+__device__ __forceinline__ void cell_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
+                                          int c, int k, int64_t i, const double *u) {
+  const int n = m.nEoC[c];
+  double ke = 0.0, dv = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int e = m.eoc[(int64_t)j * m.nC + c];
+    const double ue = u[(int64_t)e * L + k];
+    ke = fma(st.kw[e], ue * ue, ke);
+    if (S.visc) dv = fma(st.sdv[(int64_t)j * m.nC + c], ue, dv);
+  }
+  const double inva = m.invAreaCell[c];
+  S.ke[i] = ke * inva;
+  // sdv = edgeSignOnCell dv is inward-positive; the divergence is outward-positive
+  if (S.visc) S.divc[i] = -dv * inva;
+}
+
+__device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
+                                            int v, int k, int64_t i, const double *u,
+                                            const double *h) {
+  double circ = 0.0, hs = 0.0;
+#pragma unroll
+  for (int j = 0; j < kVertexDegree; ++j) {
+    const int64_t s = (int64_t)j * m.nV + v;
+    circ = fma(st.sdc[s], u[(int64_t)m.eov[s] * L + k], circ);
+    hs = fma(m.kite[s], h[(int64_t)m.cov[s] * L + k], hs);
+  }
+  S.vort[i] = circ * m.invAreaTriangle[v];
+  // (f + circ/A) / (hs/A) = (f A + circ) / hs
+  S.pv[i] = fma(m.fVertex[v], m.areaTriangle[v], circ) * rcp_nr(hs);
+}
+
+// ------------------------------------------------------ K3: cells + vertices
+template <int T>
+__global__ void __launch_bounds__(TPB) k_sw_final(DMesh m, DStat st, Stage S, int L) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  const double *u_next = S.stage == 3 ? S.u_new : S.u_out;
+  const double *h_next = S.stage == 3 ? S.h_new : S.h_out;
+  if (i < nCL) {
+    const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+    if constexpr (T > 0) {
+      double tend[T];
+      cell_tracer_tend<T>(m, S, L, c, k, i, tend);
+      const double rh = rcp_nr(h_next[i]);
+      const double hpv = S.h_prev[i];
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        // thickness-weighted tracer RK (apps/sw/tasks/solve.cc:162, 300-302, 337, 354)
+        const double hp_tp = hpv * S.tr_prev[i * T + t];
+        switch (S.stage) {
+          case 0:
+            S.tr_out[i * T + t] = fma(S.w_sub, tend[t], hp_tp) * rh;
+            S.trh_acc[i * T + t] = fma(S.w_acc, tend[t], hp_tp);
+            break;
+          case 3:
+            S.tr_new[i * T + t] = fma(S.w_acc, tend[t], S.trh_acc[i * T + t]) * rh;
+            break;
+          default:
+            S.tr_out[i * T + t] = fma(S.w_sub, tend[t], hp_tp) * rh;
+            S.trh_acc[i * T + t] = fma(S.w_acc, tend[t], S.trh_acc[i * T + t]);
+        }
+      }
+    }
+    cell_diag(m, st, S, L, c, k, i, u_next);
+    return;
+  }
+  i -= nCL;
+  if (i >= (int64_t)m.nV * L) return;
+  const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
+  vertex_diag(m, st, S, L, v, k, i, u_next, h_next);
+}
+
+// Initial diagnostics (apps/sw/run.cc:226-230).
+__global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int L) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (i < nCL) {
+    const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+    cell_diag(m, st, S, L, c, k, i, S.u_in);
+    return;
+  }
+  i -= nCL;
+  if (i >= (int64_t)m.nV * L) return;
+  const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
+  vertex_diag(m, st, S, L, v, k, i, S.u_in, S.h_in);
+}
+
+// Derived statics of a state.
+__global__ void k_build_stat(DMesh m, double kappa, double *sdv, double *kw, double *sdc,
+                             double *dhs, double *kd) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < (int64_t)m.maxEoC * m.nC) {
+    const int c = (int)(i % m.nC), j = (int)(i / m.nC);
+    sdv[i] = j < m.nEoC[c] ? m.eocSign[i] * m.dvEdge[m.eoc[i]] : 0.0;
+  }
+  if (i < m.nE) {
+    kw[i] = 0.25 * m.dcEdge[i] * m.dvEdge[i];
+    const int2 c = m.coe[i];
+    dhs[i] = m.bottomDepth[c.y] - m.bottomDepth[c.x];
+    kd[i] = m.meshScalingDel2[i] * kappa * m.dvEdge[i] * m.invDcEdge[i];
+  }
+  if (i < (int64_t)kVertexDegree * m.nV) sdc[i] = m.eovSign[i] * m.dcEdge[m.eov[i]];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ state context
+SwState::~SwState() {
+  if (graph) cudaGraphExecDestroy(graph);
+  if (arena) cudaFree(arena);
+}
+
+void alloc_arena(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs) {
+  size_t total = 0;
+  for (auto &b : bufs) total += ((size_t)std::max<int64_t>(b.second, 1) * 8 + 255) & ~size_t(255);
+  if (cudaMalloc(&s.arena, total) != cudaSuccess) {
+    cudaGetLastError();
+    fail(MPASO_ERR_ALLOC, "device allocation of the state failed (" + std::to_string(total) + " bytes)");
+  }
+  s.arena_bytes = total;
+  MPASO_CUDA(cudaMemsetAsync(s.arena, 0, total, s.stream));
+  char *p = (char *)s.arena;
+  for (auto &b : bufs) {
+    *b.first = (double *)p;
+    p += ((size_t)std::max<int64_t>(b.second, 1) * 8 + 255) & ~size_t(255);
+  }
+}
+
+void build_stat(SwState &s) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t nmax = std::max<int64_t>(std::max<int64_t>(m.nE, 3LL * m.nV), (int64_t)m.maxEoC * m.nC);
+  k_build_stat<<<blocks_for(nmax, TPB), TPB, 0, s.stream>>>(
+      m, s.p.kappa, (double *)s.st.sdv, (double *)s.st.kw, (double *)s.st.sdc, (double *)s.st.dhs,
+      (double *)s.st.kd);
+  MPASO_CUDA(cudaGetLastError());
+}
+
+namespace {
+
+Stage make_stage(SwState &s, int rk, double dt) {
+  const double rk_w[4] = {dt / 6, dt / 3, dt / 3, dt / 6};  // apps/sw/run.cc:23-24
+  const double rk_sub[4] = {dt / 2, dt / 2, dt, 0};
+  Stage S{};
+  S.stage = rk, S.w_sub = rk_sub[rk], S.w_acc = rk_w[rk], S.dt = dt, S.g = s.p.gravity, S.nu = s.p.nu;
+  S.fct = s.p.fct, S.hmix = s.p.hmix, S.visc = s.p.nu != 0.0, S.pin_u = s.p.pin_u;
+  // buffer rotation: prev = 0, acc = 2, stage inputs 0 -> 1 -> 3 -> 1, new -> 0
+  static const int uin[4] = {0, 1, 3, 1}, uout[4] = {1, 3, 1, -1};
+  S.u_in = s.U[uin[rk]], S.h_in = s.H[uin[rk]];
+  S.u_prev = s.U[0], S.h_prev = s.H[0], S.tr_prev = s.TR0;
+  S.u_out = uout[rk] >= 0 ? s.U[uout[rk]] : nullptr;
+  S.h_out = uout[rk] >= 0 ? s.H[uout[rk]] : nullptr;
+  double *trs[4] = {s.TR0, s.TRA, s.TRB, s.TRA};
+  S.tr_in = trs[rk];
+  S.tr_out = rk < 3 ? trs[rk + 1] : nullptr;
+  S.u_acc = s.U[2], S.h_acc = s.H[2], S.trh_acc = s.TRH;
+  S.u_new = s.U[0], S.h_new = s.H[0], S.tr_new = s.TR0;
+  S.pv = s.pv, S.vort = s.vort, S.ke = s.ke, S.divc = s.divc;
+  S.F = s.F, S.G = s.G, S.pve = s.pve, S.A = s.A, S.LO = s.LO, S.DF = s.DF;
+  S.Rp = s.Rp, S.Rm = s.Rm, S.tLO = s.tLO;
+  return S;
+}
+
+template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int L = s.L;
+  k_sw_edge_pre<T><<<blocks_for((int64_t)m.nE * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  k_sw_tend<T><<<blocks_for(((int64_t)m.nE + m.nC) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  k_sw_final<T><<<blocks_for(((int64_t)m.nC + m.nV) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+}
+
+void launch_stage(SwState &s, const Stage &S, cudaStream_t st) {
+  switch (s.T) {
+    case 0: launch_stage_T<0>(s, S, st); break;
+    case 1: launch_stage_T<1>(s, S, st); break;
+    case 2: launch_stage_T<2>(s, S, st); break;
+    case 3: launch_stage_T<3>(s, S, st); break;
+    case 4: launch_stage_T<4>(s, S, st); break;
+    case 5: launch_stage_T<5>(s, S, st); break;
+    case 6: launch_stage_T<6>(s, S, st); break;
+    case 7: launch_stage_T<7>(s, S, st); break;
+    case 8: launch_stage_T<8>(s, S, st); break;
+    default: fail(MPASO_ERR_ARG, "ntr out of range");
+  }
+}
+
+void ensure_diag(SwState &s, cudaStream_t st) {
+  if (s.diag_valid) return;
+  const DMesh &m = s.mesh->ctx.d;
+  Stage S = make_stage(s, 0, 0.0);
+  k_sw_diag<<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+  MPASO_CUDA(cudaGetLastError());
+  s.diag_valid = true;
+}
+
+void sw_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
+  ensure_diag(s, st);
+  for (int n = 0; n < nsteps; ++n)
+    for (int rk = 0; rk < 4; ++rk) launch_stage(s, make_stage(s, rk, dt), st);
+  MPASO_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+// Entry points of the ocean path (ocean.cu).
+void ocean_create(SwState &s);
+void ocean_steps(SwState &s, double dt, int nsteps, cudaStream_t st);
+void ocean_prepare(SwState &s, double dt, cudaStream_t st);
+int ocean_launches_per_step(const SwState &s);
+
+void sw_create(SwState &s) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t L = s.L, T = s.T;
+  const int64_t nC = m.nC, nE = m.nE, nV = m.nV;
+  std::vector<std::pair<double **, int64_t>> bufs = {
+      {&s.U[0], nE * L}, {&s.U[1], nE * L}, {&s.U[2], nE * L}, {&s.U[3], nE * L},
+      {&s.H[0], nC * L}, {&s.H[1], nC * L}, {&s.H[2], nC * L}, {&s.H[3], nC * L},
+      {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
+      {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.ke, nC * L}, {&s.divc, nC * L},
+      {&s.F, nE * L}, {&s.G, nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
+      {&s.DF, nE * L * T}, {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T},
+      {(double **)&s.st.sdv, (int64_t)m.maxEoC * nC}, {(double **)&s.st.kw, nE},
+      {(double **)&s.st.sdc, 3 * nV}, {(double **)&s.st.dhs, nE}, {(double **)&s.st.kd, nE}};
+  alloc_arena(s, bufs);
+  build_stat(s);
+}
+
+}  // namespace mpaso
+
+struct mpaso_state_s {
+  mpaso::SwState s;
+};
+
+using namespace mpaso;
+
+namespace {
+
+void field_geom(SwState &s, int field, int &entity, int64_t &row, double *&buf) {
+  switch (field) {
+    case MPASO_FIELD_H: entity = MPASO_CELLS, row = s.L, buf = s.H[0]; break;
+    case MPASO_FIELD_U: entity = MPASO_EDGES, row = s.L, buf = s.U[0]; break;
+    case MPASO_FIELD_TRACERS: entity = MPASO_CELLS, row = (int64_t)s.L * s.T, buf = s.TR0; break;
+    case MPASO_FIELD_LAYER_THICKNESS_EDGE:
+      require(s.p.app == MPASO_APP_OCEAN, MPASO_ERR_ARG, "layerThicknessEdge is an ocean field");
+      entity = MPASO_EDGES, row = s.L, buf = s.HE;
+      break;
+    default: fail(MPASO_ERR_ARG, "unknown field id");
+  }
+  require(row > 0, MPASO_ERR_ARG, "field has no data (ntr = 0?)");
+}
+
+void run_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
+  if (s.p.app == MPASO_APP_OCEAN)
+    ocean_steps(s, dt, nsteps, st);
+  else
+    sw_steps(s, dt, nsteps, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpaso_state_create(mpaso_mesh m, const mpaso_params *p, mpaso_state *out) {
+  return guarded("mpaso_state_create", [&] {
+    require(m && p && out, MPASO_ERR_ARG, "null argument");
+    require(p->nlev >= 1 && p->nlev <= 4096, MPASO_ERR_ARG, "nlev out of range");
+    require(p->ntr >= 0 && p->ntr <= kMaxTracers, MPASO_ERR_ARG, "ntr out of range (max 8)");
+    require(p->app == MPASO_APP_SW || p->app == MPASO_APP_OCEAN, MPASO_ERR_ARG, "unknown app");
+    if (p->fct) {
+      require(m->ctx.has_fct, MPASO_ERR_ARG, "fct requested but the mesh has no FCT statics");
+      require(m->ctx.d.fctLev == p->nlev, MPASO_ERR_ARG, "FCT statics built for another level count");
+      std::vector<int> mlc(m->ctx.d.nC);
+      MPASO_CUDA(cudaMemcpy(mlc.data(), m->ctx.d.maxLevelCell, mlc.size() * sizeof(int), cudaMemcpyDeviceToHost));
+      for (int x : mlc)
+        require(x == p->nlev, MPASO_ERR_ARG, "fused path needs maxLevelCell == nlev in every cell");
+    }
+    if (p->app == MPASO_APP_OCEAN) require(p->ntr >= 1, MPASO_ERR_ARG, "ocean app needs tracers");
+    MPASO_CUDA(cudaSetDevice(m->ctx.device));
+    auto *h = new mpaso_state_s();
+    try {
+      SwState &s = h->s;
+      s.mesh = m, s.p = *p, s.L = p->nlev, s.T = p->ntr;
+      MPASO_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+      if (p->app == MPASO_APP_OCEAN)
+        ocean_create(s);
+      else
+        sw_create(s);
+      MPASO_CUDA(cudaStreamSynchronize(s.stream));
+    } catch (...) {
+      if (h->s.stream) cudaStreamDestroy(h->s.stream);
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int mpaso_state_destroy(mpaso_state s) {
+  return guarded("mpaso_state_destroy", [&] {
+    if (!s) return;
+    cudaSetDevice(s->s.mesh->ctx.device);
+    cudaStreamSynchronize(s->s.stream);
+    cudaStream_t st = s->s.stream;
+    delete s;
+    cudaStreamDestroy(st);
+  });
+}
+
+int mpaso_state_set(mpaso_state s, int32_t field, const double *data) {
+  return guarded("mpaso_state_set", [&] {
+    require(s && data, MPASO_ERR_ARG, "null argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    int entity;
+    int64_t row;
+    double *buf;
+    field_geom(S, field, entity, row, buf);
+    MeshCtx &ctx = S.mesh->ctx;
+    const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : entity == MPASO_EDGES ? ctx.d.nE : ctx.d.nV;
+    const double *src = data;
+    double *stage = nullptr;
+    if (!is_device_pointer(data)) {
+      MPASO_CUDA(cudaMallocAsync((void **)&stage, (size_t)n * row * 8, S.stream));
+      MPASO_CUDA(cudaMemcpyAsync(stage, data, (size_t)n * row * 8, cudaMemcpyHostToDevice, S.stream));
+      src = stage;
+    }
+    k_gather_rows_pub(src, buf, ctx.d_perm[entity], n, (int)row, S.stream);
+    if (stage) MPASO_CUDA(cudaFreeAsync(stage, S.stream));
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+    S.diag_valid = false;
+    S.prep_dt = 0.0;
+  });
+}
+
+int mpaso_state_get(mpaso_state s, int32_t field, double *data) {
+  return guarded("mpaso_state_get", [&] {
+    require(s && data, MPASO_ERR_ARG, "null argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    int entity;
+    int64_t row;
+    double *buf;
+    field_geom(S, field, entity, row, buf);
+    MeshCtx &ctx = S.mesh->ctx;
+    const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : entity == MPASO_EDGES ? ctx.d.nE : ctx.d.nV;
+    const bool dev = is_device_pointer(data);
+    double *dst = data;
+    if (!dev) MPASO_CUDA(cudaMallocAsync((void **)&dst, (size_t)n * row * 8, S.stream));
+    k_scatter_rows_pub(buf, dst, ctx.d_perm[entity], n, (int)row, S.stream);
+    if (!dev) {
+      MPASO_CUDA(cudaMemcpyAsync(data, dst, (size_t)n * row * 8, cudaMemcpyDeviceToHost, S.stream));
+      MPASO_CUDA(cudaFreeAsync(dst, S.stream));
+    }
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+  });
+}
+
+int mpaso_rk4_step(mpaso_state s, double dt, int32_t nsteps) {
+  return guarded("mpaso_rk4_step", [&] {
+    require(s != nullptr && nsteps >= 0, MPASO_ERR_ARG, "bad argument");
+    MPASO_CUDA(cudaSetDevice(s->s.mesh->ctx.device));
+    run_steps(s->s, dt, nsteps, s->s.stream);
+  });
+}
+
+int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps) {
+  return guarded("mpaso_rk4_step_graph", [&] {
+    require(s != nullptr && nsteps >= 0, MPASO_ERR_ARG, "bad argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    if (S.p.app == MPASO_APP_SW)
+      ensure_diag(S, S.stream);
+    else
+      ocean_prepare(S, dt, S.stream);
+    if (!S.graph || S.graph_dt != dt) {
+      if (S.graph) {
+        MPASO_CUDA(cudaGraphExecDestroy(S.graph));
+        S.graph = nullptr;
+      }
+      cudaGraph_t g;
+      MPASO_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        run_steps(S, dt, 1, S.stream);
+      } catch (...) {
+        cudaStreamEndCapture(S.stream, &g);
+        cudaGetLastError();
+        throw;
+      }
+      MPASO_CUDA(cudaStreamEndCapture(S.stream, &g));
+      MPASO_CUDA(cudaGraphInstantiate(&S.graph, g, 0));
+      MPASO_CUDA(cudaGraphDestroy(g));
+      S.graph_dt = dt;
+    }
+    for (int n = 0; n < nsteps; ++n) MPASO_CUDA(cudaGraphLaunch(S.graph, S.stream));
+  });
+}
+
+int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                        double *tracers) {
+  int rc = mpaso_state_set(s, MPASO_FIELD_H, h);
+  if (!rc) rc = mpaso_state_set(s, MPASO_FIELD_U, u);
+  if (!rc && tracers && s->s.T > 0) rc = mpaso_state_set(s, MPASO_FIELD_TRACERS, tracers);
+  if (!rc) rc = mpaso_rk4_step_graph(s, dt, nsteps);
+  if (!rc) rc = mpaso_state_get(s, MPASO_FIELD_H, h);
+  if (!rc) rc = mpaso_state_get(s, MPASO_FIELD_U, u);
+  if (!rc && tracers && s->s.T > 0) rc = mpaso_state_get(s, MPASO_FIELD_TRACERS, tracers);
+  return rc;
+}
+
+int mpaso_state_sync(mpaso_state s) {
+  return guarded("mpaso_state_sync", [&] {
+    require(s != nullptr, MPASO_ERR_ARG, "null state");
+    MPASO_CUDA(cudaStreamSynchronize(s->s.stream));
+  });
+}
+
+int mpaso_state_stream(mpaso_state s, void **stream) {
+  return guarded("mpaso_state_stream", [&] {
+    require(s && stream, MPASO_ERR_ARG, "null argument");
+    *stream = (void *)s->s.stream;
+  });
+}
+
+int mpaso_state_launches_per_step(mpaso_state s, int32_t *n) {
+  return guarded("mpaso_state_launches_per_step", [&] {
+    require(s && n, MPASO_ERR_ARG, "null argument");
+    *n = s->s.p.app == MPASO_APP_OCEAN ? ocean_launches_per_step(s->s) : 12;
+  });
+}
+
+int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes) {
+  return guarded("mpaso_state_device_bytes", [&] {
+    require(s && bytes, MPASO_ERR_ARG, "null argument");
+    *bytes = (int64_t)s->s.arena_bytes;
+  });
+}
+
+}  // extern "C"

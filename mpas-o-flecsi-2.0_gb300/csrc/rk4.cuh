@@ -1,0 +1,213 @@
+// Fused RK4 path: state context, stage parameters and the FCT / del2 device
+// code shared by the sw driver (rk4.cu) and the ocean tracer driver (ocean.cu).
+#pragma once
+
+#include <vector>
+
+#include "device.cuh"
+#include "task_io.cuh"
+
+namespace mpaso {
+
+constexpr long long kSignBit = (long long)0x8000000000000000ULL;
+
+// Fast FP64 reciprocal: hardware approximation (rcp.approx.ftz.f64) refined
+// by two Newton-Raphson steps r <- r + r (1 - b r); within a few ulp of 1/b
+// for normal b.
+__device__ __forceinline__ double rcp_nr(double b) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));
+  double e = fma(-b, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-b, r, 1.0);
+  return fma(r, e, r);
+}
+
+__device__ __forceinline__ long long sign_mask(double s) { return dbits(s) & kSignBit; }
+
+// Per-state derived statics (device arrays), built once at state creation.
+struct DStat {
+  const double *sdv;  // [maxEoC][nC] edgeSignOnCell * dvEdge (0 in pad slots)
+  const double *kw;   // [nE] 0.25 * dcEdge * dvEdge
+  const double *sdc;  // [3][nV] circulation sign * dcEdge
+  const double *dhs;  // [nE] h_s(c2) - h_s(c1)
+  const double *kd;   // [nE] meshScalingDel2 * kappa * dvEdge / dcEdge
+};
+
+// One RK stage's pointers and weights.
+struct Stage {
+  int stage;            // 0..3
+  double w_sub, w_acc;  // substep and accumulation weights (apps/sw/run.cc:23-24)
+  double dt, g, nu;
+  int fct, hmix, visc, pin_u;
+  const double *u_in, *h_in, *tr_in;        // stage input
+  const double *u_prev, *h_prev, *tr_prev;  // step start
+  double *u_out, *h_out, *tr_out;           // next stage input (stages 0..2)
+  double *u_acc, *h_acc, *trh_acc;          // RK accumulators
+  double *u_new, *h_new, *tr_new;           // step result (stage 3)
+  double *pv, *vort, *ke, *divc;            // diagnostics of the stage input
+  double *F, *G, *pve, *A, *LO, *DF;        // edge intermediates
+  double *Rp, *Rm, *tLO;                    // cell intermediates
+  const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
+};
+
+// State context (sw or ocean app).
+struct SwState {
+  mpaso_mesh mesh = nullptr;
+  mpaso_params p{};
+  int L = 1, T = 0;
+  cudaStream_t stream = nullptr;
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  double *U[4]{}, *H[4]{}, *TR0 = nullptr, *TRA = nullptr, *TRB = nullptr, *TRH = nullptr;
+  double *HE = nullptr, *HPI = nullptr;
+  double *pv = nullptr, *vort = nullptr, *ke = nullptr, *divc = nullptr;
+  double *F = nullptr, *G = nullptr, *pve = nullptr, *A = nullptr, *LO = nullptr, *DF = nullptr;
+  double *Rp = nullptr, *Rm = nullptr, *tLO = nullptr;
+  DStat st{};
+  bool diag_valid = false;  // sw: diagnostics of U[0]/H[0] current
+  double prep_dt = 0.0;     // ocean: dt of the cached F / 1/hProv (0 = stale)
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = 0.0;
+  ~SwState();
+};
+
+// Allocates the state buffers listed as (pointer, doubles) in one arena.
+void alloc_arena(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs);
+void build_stat(SwState &s);
+
+// ---------------------------------------------------------------------------
+// FCT / del2 tracer device code (apps/ocean/tasks/solve.cc:99-366).
+
+// Edge fluxes for tracers of the stage input: low-order flux LO, anti-
+// diffusive flux A = HO - LO, del2 flux DF = h_e (tr2 - tr1) kappa ...
+template <int T>
+__device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const DStat &st, const Stage &S,
+                                                   int L, int e, int k, int64_t i, int64_t i1,
+                                                   int64_t i2, double F, double he) {
+  double t1[T], t2[T];
+#pragma unroll
+  for (int t = 0; t < T; ++t) t1[t] = S.tr_in[i1 * T + t], t2[t] = S.tr_in[i2 * T + t];
+  const double dvF = m.dvEdge[e] * F;
+  if (S.fct) {
+    // low order: dv (max(0,F) tr1 + min(0,F) tr2) == dv F tr_upwind (ocean solve.cc:110-113)
+    const bool up1 = dgt0(F);
+    // high order: F mask sum_a tr_a (advCoef_a + 0.25 advCoef_3rd_a sign(F)) (solve.cc:137-165)
+    const double *coef = dlt0(F) ? m.advCm : m.advCp;
+    double s[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) s[t] = 0.0;
+    for (int a = 0; a < m.maxAdv; ++a) {
+      const int cell = m.advCells[(int64_t)a * m.nE + e];
+      const double cf = coef[(int64_t)a * m.nE + e];
+      const double *tr = S.tr_in + ((int64_t)cell * L + k) * T;
+#pragma unroll
+      for (int t = 0; t < T; ++t) s[t] = fma(cf, tr[t], s[t]);
+    }
+    const int mask = m.hoMask[(int64_t)e * m.fctLev + k];
+    const double wgt = mask ? F : 0.0;
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      const double lo = dvF * (up1 ? t1[t] : t2[t]);
+      double ho = wgt * s[t];
+      if (!mask) ho = fma(0.5 * dvF, t1[t] + t2[t], ho);  // solve.cc:222-225
+      S.LO[i * T + t] = lo;
+      S.A[i * T + t] = ho - lo;
+    }
+  } else {
+    // centred flux of compute_scalar_tend (apps/sw/tasks/solve.cc:255-269)
+#pragma unroll
+    for (int t = 0; t < T; ++t) S.LO[i * T + t] = (0.5 * dvF) * (t1[t] + t2[t]);
+  }
+  if (S.hmix) {
+    const double hk = he * st.kd[e];
+#pragma unroll
+    for (int t = 0; t < T; ++t) S.DF[i * T + t] = hk * (t2[t] - t1[t]);
+  }
+}
+
+// Cell bounds, upwind tendency and limiter factors R+ / R- (ocean solve.cc:194-267).
+template <int T>
+__device__ __forceinline__ void cell_limiter(const DMesh &m, const Stage &S, int L, int c, int k,
+                                             int64_t i, double hin, double hpi) {
+  const int n = m.nEoC[c];
+  const double inva = m.invAreaCell[c];
+  if (!S.fct) {
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      double tl = 0.0;
+      for (int j = 0; j < n; ++j) {
+        const int e = m.eoc[(int64_t)j * m.nC + c];
+        tl += dflip(S.LO[((int64_t)e * L + k) * T + t], sign_mask(m.eocSign[(int64_t)j * m.nC + c]));
+      }
+      S.tLO[i * T + t] = tl * inva;
+    }
+    return;
+  }
+  const double dth = S.dt * hpi;
+  const double eps = 1.e-10;
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const double trc = S.tr_in[i * T + t];
+    double mx = trc, mn = trc, tl = 0.0, fi = 0.0, fo = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int nb = m.coc[(int64_t)j * m.nC + c];
+      const double x = S.tr_in[((int64_t)nb * L + k) * T + t];
+      mx = dmax(mx, x);
+      mn = dmin(mn, x);
+      const int e = m.eoc[(int64_t)j * m.nC + c];
+      const long long sm = sign_mask(m.eocSign[(int64_t)j * m.nC + c]);
+      const int64_t ie = ((int64_t)e * L + k) * T + t;
+      tl += dflip(S.LO[ie], sm);
+      const double ax = dflip(S.A[ie], sm);
+      fi += dpos(ax);
+      fo += dneg(ax);
+    }
+    tl *= inva;
+    fi *= inva;
+    fo *= inva;
+    const double up = fma(S.dt, tl, trc * hin) * hpi;
+    const double mxn = fma(dth, fi, up), mnn = fma(dth, fo, up);
+    const double np = mx - up, dp = (mxn - up) + eps;
+    const double nm = up - mn, dm = (up - mnn) + eps;
+    // clamp01(n / d): 0 when n <= 0, 1 when n >= d, the quotient otherwise
+    double rp = dgt0(np) ? 1.0 : 0.0, rm = dgt0(nm) ? 1.0 : 0.0;
+    if (dgt0(np) && dkey(np) < dkey(dp)) rp = dclamp01(np * rcp_nr(dp));
+    if (dgt0(nm) && dkey(nm) < dkey(dm)) rm = dclamp01(nm * rcp_nr(dm));
+    S.Rp[i * T + t] = rp;
+    S.Rm[i * T + t] = rm;
+    S.tLO[i * T + t] = tl;
+  }
+}
+
+// Tracer tendency of a cell: upwind part + limited anti-diffusive fluxes
+// (ocean solve.cc:269-326) - del2 mixing (solve.cc:340-364).
+template <int T>
+__device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S, int L, int c,
+                                                 int k, int64_t i, double *tend) {
+  const int n = m.nEoC[c];
+  const double inva = m.invAreaCell[c];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int e = m.eoc[(int64_t)j * m.nC + c];
+      const long long sm = sign_mask(m.eocSign[(int64_t)j * m.nC + c]);
+      const int64_t ie = ((int64_t)e * L + k) * T + t;
+      double x = 0.0;
+      if (S.fct) {
+        const int2 cc = m.coe[e];
+        const int64_t j1 = ((int64_t)cc.x * L + k) * T + t, j2 = ((int64_t)cc.y * L + k) * T + t;
+        const double a = S.A[ie];
+        // max(0,A) min(R-(c1), R+(c2)) + min(0,A) min(R+(c1), R-(c2))  (solve.cc:276-279)
+        const double r = dgt0(a) ? dmin(S.Rm[j1], S.Rp[j2]) : dmin(S.Rp[j1], S.Rm[j2]);
+        x = a * r;
+      }
+      if (S.hmix) x -= S.DF[ie];
+      acc += dflip(x, sm);
+    }
+    tend[t] = fma(inva, acc, S.tLO[i * T + t]);
+  }
+}
+
+}  // namespace mpaso

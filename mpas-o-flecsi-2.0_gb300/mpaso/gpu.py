@@ -1,0 +1,239 @@
+"""ctypes binding of the device path (include/mpaso.h).
+
+Arrays may be numpy arrays (host memory) or any object with `data_ptr()` /
+`__cuda_array_interface__` pointing at device memory (e.g. torch CUDA
+tensors); the library detects which.  All arrays use the reference's entity
+numbering and per-entity AoS rows.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import check, lib
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_lp = ctypes.POINTER(ctypes.c_int64)
+
+CELLS, EDGES, VERTICES = 0, 1, 2
+APP_SW, APP_OCEAN = 0, 1
+FIELD_H, FIELD_U, FIELD_TRACERS, FIELD_LAYER_THICKNESS_EDGE = 0, 1, 2, 3
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = ([("nCells", ctypes.c_int64), ("nEdges", ctypes.c_int64), ("nVertices", ctypes.c_int64)]
+                + [(n, _lp) for n in ("c2v_off", "c2e_off", "c2c_off", "e2v_off", "e2e_off")]
+                + [(n, _ip) for n in ("c2v", "c2e", "c2c", "e2v", "e2e")]
+                + [(n, _dp) for n in ("areaCell", "dvEdge", "dcEdge", "areaTriangle",
+                                      "kiteAreasOnVertex", "fVertex", "weightsOnEdge", "bottomDepth",
+                                      "xCell", "yCell", "zCell")]
+                + [("reorder", ctypes.c_int32), ("fct_nlev", ctypes.c_int32)]
+                + [(n, _ip) for n in ("maxLevelCell", "maxLevelEdgeTop", "nAdvCellsForEdge",
+                                      "advCellsForEdge", "highOrderAdvMask")]
+                + [(n, _dp) for n in ("edgeSignOnCell", "advCoef", "advCoef_3rd", "meshScalingDel2")])
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("app", ctypes.c_int32), ("nlev", ctypes.c_int32), ("ntr", ctypes.c_int32),
+                ("gravity", ctypes.c_double), ("fct", ctypes.c_int32), ("hmix", ctypes.c_int32),
+                ("kappa", ctypes.c_double), ("nu", ctypes.c_double), ("pin_u", ctypes.c_int32)]
+
+
+def _np_ptr(a, kind):
+    return a.ctypes.data_as(kind)
+
+
+def _ptr(a):
+    """Raw address of a numpy array or a device tensor."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return ctypes.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        if hasattr(a, "is_contiguous") and not a.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return ctypes.c_void_p(a.data_ptr())
+    if hasattr(a, "__cuda_array_interface__"):
+        return ctypes.c_void_p(a.__cuda_array_interface__["data"][0])
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def device_count():
+    n = ctypes.c_int32()
+    check(lib().mpaso_device_count(ctypes.byref(n)))
+    return n.value
+
+
+class DeviceMesh:
+    """Device mesh context built from a generated mpaso.Mesh (reference semantics)."""
+
+    def __init__(self, mesh, fct=None, bottomDepth=None, reorder=True, device=0):
+        crs = mesh.crs()
+        f = mesh.fields
+        keep = {}
+
+        def arr(name, a, dtype):
+            a = np.ascontiguousarray(a, dtype)
+            keep[name] = a
+            return _np_ptr(a, _dp if dtype == np.float64 else (_ip if dtype == np.int32 else _lp))
+
+        d = MeshDesc()
+        d.nCells, d.nEdges, d.nVertices = mesh.nCells, mesh.nEdges, mesh.nVertices
+        for n in ("c2v", "c2e", "c2c", "e2v", "e2e"):
+            off, idx = crs[n]
+            setattr(d, n + "_off", arr(n + "_off", off, np.int64))
+            setattr(d, n, arr(n, idx, np.int32))
+        for n in ("areaCell", "dvEdge", "dcEdge", "areaTriangle", "kiteAreasOnVertex", "fVertex",
+                  "weightsOnEdge", "xCell", "yCell", "zCell"):
+            setattr(d, n, arr(n, f[n], np.float64))
+        if bottomDepth is not None:
+            d.bottomDepth = arr("bottomDepth", bottomDepth, np.float64)
+        d.reorder = 1 if reorder else 0
+        if fct is not None:
+            d.fct_nlev = fct["highOrderAdvMask"].shape[1]
+            for n in ("maxLevelCell", "maxLevelEdgeTop", "nAdvCellsForEdge", "advCellsForEdge",
+                      "highOrderAdvMask"):
+                setattr(d, n, arr(n, fct[n], np.int32))
+            for n in ("edgeSignOnCell", "advCoef", "advCoef_3rd", "meshScalingDel2"):
+                setattr(d, n, arr(n, fct[n], np.float64))
+        self._h = ctypes.c_void_p()
+        check(lib().mpaso_mesh_create(ctypes.byref(d), int(device), ctypes.byref(self._h)))
+        self.mesh = mesh
+        self.nC, self.nE, self.nV = mesh.nCells, mesh.nEdges, mesh.nVertices
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mpaso_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def permutation(self, entity):
+        n = (self.nC, self.nE, self.nV)[entity]
+        out = np.empty(n, np.int32)
+        check(lib().mpaso_mesh_permutation(self._h, int(entity), _np_ptr(out, _ip)))
+        return out
+
+    def set_gravity(self, g):
+        check(lib().mpaso_mesh_set_gravity(self._h, ctypes.c_double(g)))
+
+    def device_bytes(self):
+        b = ctypes.c_int64()
+        check(lib().mpaso_mesh_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    # ---- per-task entries: return outputs as new numpy arrays ----
+    def _call(self, name, *args):
+        conv = [self._h]
+        for a in args:
+            if isinstance(a, float):
+                conv.append(ctypes.c_double(a))
+            elif isinstance(a, int):
+                conv.append(ctypes.c_int32(a))
+            else:
+                conv.append(_ptr(a))
+        conv.append(None)  # stream: the context's own
+        check(getattr(lib(), "mpaso_" + name)(*conv))
+
+    def sw_compute_solve_diagnostics(self, L, h, u, out=None):
+        o = out or {k: np.zeros((n, L)) for k, n in (("h_edge", self.nE), ("h_vertex", self.nV),
+                                                     ("circulation", self.nV), ("vorticity", self.nV),
+                                                     ("ke", self.nC), ("pv_edge", self.nE),
+                                                     ("pv_vertex", self.nV))}
+        self._call("sw_compute_solve_diagnostics", L, h, u, o["h_edge"], o["h_vertex"],
+                   o["circulation"], o["vorticity"], o["ke"], o["pv_edge"], o["pv_vertex"])
+        return o
+
+    def sw_compute_tend(self, L, h_edge, h, u, ke, pv_edge):
+        th, tu = np.zeros((self.nC, L)), np.zeros((self.nE, L))
+        self._call("sw_compute_tend", L, h_edge, h, u, ke, pv_edge, th, tu)
+        return th, tu
+
+    def sw_compute_scalar_tend(self, L, T, h_edge, u, tracers):
+        out = np.zeros((self.nC, L, T))
+        self._call("sw_compute_scalar_tend", L, T, h_edge, u, tracers, out)
+        return out
+
+    def call(self, name, *args):
+        """Generic per-task call: mpaso_<name>(mesh, *args, stream=NULL)."""
+        self._call(name, *args)
+
+
+class State:
+    """Device-resident state of the fused RK4 path."""
+
+    def __init__(self, dmesh, app=APP_SW, nlev=1, ntr=1, gravity=9.80616, fct=False, hmix=False,
+                 kappa=0.0, nu=0.0, pin_u=False):
+        self.dmesh = dmesh
+        self.L, self.T, self.app = nlev, ntr, app
+        p = Params(app, nlev, ntr, gravity, int(fct), int(hmix), kappa, nu, int(pin_u))
+        self._h = ctypes.c_void_p()
+        check(lib().mpaso_state_create(dmesh.handle, ctypes.byref(p), ctypes.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mpaso_state_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _shape(self, field):
+        dm = self.dmesh
+        return {FIELD_H: (dm.nC, self.L), FIELD_U: (dm.nE, self.L),
+                FIELD_TRACERS: (dm.nC, self.L, self.T),
+                FIELD_LAYER_THICKNESS_EDGE: (dm.nE, self.L)}[field]
+
+    def set(self, field, data):
+        if isinstance(data, np.ndarray):
+            data = np.ascontiguousarray(data, np.float64)
+            if data.size != int(np.prod(self._shape(field))):
+                raise ValueError("field size mismatch")
+        check(lib().mpaso_state_set(self._h, int(field), _ptr(data)))
+
+    def get(self, field, out=None):
+        out = np.empty(self._shape(field)) if out is None else out
+        check(lib().mpaso_state_get(self._h, int(field), _ptr(out)))
+        return out
+
+    def step(self, dt, nsteps=1):
+        check(lib().mpaso_rk4_step(self._h, ctypes.c_double(dt), int(nsteps)))
+
+    def step_graph(self, dt, nsteps=1):
+        check(lib().mpaso_rk4_step_graph(self._h, ctypes.c_double(dt), int(nsteps)))
+
+    def step_host(self, dt, nsteps, h, u, tracers):
+        """One boundary call with host buffers (copied in and back out, in place)."""
+        check(lib().mpaso_rk4_step_host(self._h, ctypes.c_double(dt), int(nsteps), _ptr(h), _ptr(u),
+                                        _ptr(tracers)))
+
+    def sync(self):
+        check(lib().mpaso_state_sync(self._h))
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().mpaso_state_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    def launches_per_step(self):
+        n = ctypes.c_int32()
+        check(lib().mpaso_state_launches_per_step(self._h, ctypes.byref(n)))
+        return n.value
+
+    def device_bytes(self):
+        b = ctypes.c_int64()
+        check(lib().mpaso_state_device_bytes(self._h, ctypes.byref(b)))
+        return b.value

@@ -26,8 +26,10 @@ VERTEX_DEGREE = 3
 
 
 class Mesh:
-    def __init__(self, handle):
+    def __init__(self, handle=None):
         self._h = handle
+        if handle is None:
+            return
         L = lib()
         dims = (ctypes.c_int64 * 3)()
         flags = (ctypes.c_int32 * 1)()
@@ -56,6 +58,23 @@ class Mesh:
                 pass
             self._h = None
 
+    # ---- (de)serialisation ----
+    def to_dict(self):
+        d = {"mesh_" + k: v for k, v in self.fields.items()}
+        d["mesh_dims"] = np.array([self.nCells, self.nEdges, self.nVertices], np.int64)
+        d["mesh_geom"] = np.array([float(self.on_sphere), self.radius, self.Lx, self.Ly])
+        return d
+
+    @classmethod
+    def from_dict(cls, d):
+        m = cls()
+        m.nCells, m.nEdges, m.nVertices = (int(x) for x in d["mesh_dims"])
+        g = d["mesh_geom"]
+        m.on_sphere, m.radius, m.Lx, m.Ly = bool(g[0]), float(g[1]), float(g[2]), float(g[3])
+        m.fields = {k[5:]: np.asarray(v) for k, v in d.items()
+                    if k.startswith("mesh_") and k not in ("mesh_dims", "mesh_geom")}
+        return m
+
     # ---- constructors ----
     @classmethod
     def icosa(cls, level, radius=EARTH_RADIUS, omega=OMEGA):
@@ -74,6 +93,8 @@ class Mesh:
     def reordered(self):
         """Same mesh regenerated in Hilbert-curve order; returns (mesh, (pc, pe, pv)) with
         perm[new] = old for cells, edges and vertices."""
+        if self._h is None:
+            raise ValueError("only generated meshes can be regenerated in curve order")
         h = ctypes.c_void_p()
         pc = np.empty(self.nCells, np.int32)
         pe = np.empty(self.nEdges, np.int32)

@@ -1,0 +1,65 @@
+"""The CPU oracle, pinned (CPU): the C restatement reproduces the reference's own
+task sources bit for bit, on the committed golden fixtures and, where the
+reference checkout was available, against the shim-compiled reference itself."""
+import numpy as np
+import pytest
+
+from helpers import Golden, golden_names
+from oracle import Oracle, ref_available
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_restatement_matches_reference_goldens(name):
+    g = Golden(name)
+    S = Oracle("restatement")
+    cfg = S.config(g.L, g.T, **g.opts)
+    st = S.static(g.mesh, g.fct)
+    for n in g.steps:
+        if g.app == "sw":
+            h, u, tr = S.sw_run(g.mesh, st, cfg, g.dt, n, g["h0"], g["u0"], g["tr0"])
+            assert np.array_equal(h, g[f"h_{n}"]) and np.array_equal(u, g[f"u_{n}"])
+            assert np.array_equal(tr, g[f"tr_{n}"])
+        else:
+            tr = S.ocean_run(g.mesh, st, cfg, g.dt, n, g["h0"], g["hE0"], g["u0"], g["tr0"])
+            assert np.array_equal(tr, g[f"tr_{n}"])
+
+
+@pytest.mark.parametrize("name", ["sw_fct_icosa3_L1T1", "ocean_icosa3_L3T2", "sw_fct_icosa2_L5T5"])
+def test_restatement_fct_statics_match_reference(name):
+    g = Golden(name)
+    S = Oracle("restatement")
+    out = S.fct_statics(g.mesh, g.L, cfg=S.config(g.L, g.T))
+    for k, v in g.fct.items():
+        assert np.array_equal(out[k], v), k
+
+
+@pytest.mark.parametrize("L,T", [(1, 1), (3, 2)])
+def test_restatement_matches_live_reference(L, T):
+    if not ref_available(L, T):
+        pytest.skip("reference checkout not built here (oracle/_ref)")
+    import mpaso
+    from mpaso.initial import sw_state
+    mesh = mpaso.Mesh.icosa(2)
+    R, S = Oracle("ref", L, T), Oracle("restatement")
+    fr = R.fct_statics(mesh, L, cfg=R.config(L, T))
+    fs = S.fct_statics(mesh, L, cfg=S.config(L, T))
+    for k in fr:
+        assert np.array_equal(fr[k], fs[k]), k
+    h, u, tr = sw_state(mesh, 99, L, T)
+    opts = dict(fct=True, hmix=True, kappa=3e4, nu=2e4)
+    a = R.sw_run(mesh, R.static(mesh, fr), R.config(L, T, **opts), 450.0, 4, h, u, tr)
+    b = S.sw_run(mesh, S.static(mesh, fs), S.config(L, T, **opts), 450.0, 4, h, u, tr)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_oracle_detects_planted_error():
+    """A mistake planted in the oracle's inputs is caught by the bit-exact comparison."""
+    g = Golden("sw_fct_icosa3_L1T1")
+    S = Oracle("restatement")
+    fct = dict(g.fct)
+    fct["advCoef"] = fct["advCoef"].copy()
+    fct["advCoef"][17, 3] *= 1.0 + 1e-6
+    h, u, tr = S.sw_run(g.mesh, S.static(g.mesh, fct), S.config(g.L, g.T, **g.opts), g.dt, 1,
+                        g["h0"], g["u0"], g["tr0"])
+    assert not np.array_equal(tr, g["tr_1"])
