@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the MPAS-O-FleCSI RK4 tendency path on GB300.
+
+Metric: RK4 cell-updates/s (one cell x one level advanced one full RK4 step),
+whole job, plus the fraction of the HBM roofline of the dominant kernel.
+
+Default workload (--config sw_l7): shallow water on the sphere, dual of a
+level-7 icosahedral subdivision (163,842 cells, 491,520 edges, 327,680
+vertices, a = 6.371e6 m), FP64, Coriolis 2 Omega sin(lat), one passive tracer
+with FCT advection, del2 tracer and momentum diffusion (1e4 m^2/s), RK4
+dt = 60 s; seeded synthetic state (degree-8 random fields: h = 8000 m +/- 100 m,
+u peak 30 m/s, tracer in [0, 1]).  Other configs: ocean_l7 (60 levels,
+3 tracers, FCT + del2 tracer only, dt = 300 s), sw_l6.
+
+Arms:
+  default           the CUDA path through the fused graph-captured RK4 step;
+  --impl reference  the reference algorithm on the host CPU cores: the
+                    reference's own task sources built through the oracle
+                    shim where they were built here, else the oracle's C
+                    restatement (bit-identical to them), one process per core.
+
+Multi-GPU (torchrun): every rank advances its own replica of the workload
+(no communication; the path has no exchange step), value = total
+cell-updates/s, "scaling": "weak".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mpas-o-flecsi-2.0_gb300")
+for _p in (PKG,):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SW RK4 cell-updates/s on 1 GB300 & % HBM roofline"
+CONFIGS = {
+    "sw_l7": dict(workload="sphere-level7 shallow-water RK4 + FCT tracer + del2 (163842 cells, L=1, T=1)",
+                  level=7, app="sw", L=1, T=1, dt=60.0, fct=True, hmix=True, kappa=1e4, nu=1e4),
+    "sw_l6": dict(workload="sphere-level6 shallow-water RK4 + FCT tracer + del2 (40962 cells, L=1, T=1)",
+                  level=6, app="sw", L=1, T=1, dt=90.0, fct=True, hmix=True, kappa=1e4, nu=1e4),
+    "ocean_l7": dict(workload="sphere-level7 ocean tracers, 60 levels x 3 tracers, FCT + del2 (9.8M cell-levels)",
+                     level=7, app="ocean", L=60, T=3, dt=300.0, fct=True, hmix=True, kappa=1e4, nu=0.0),
+}
+L2_BYTES = 129e6
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def build_workload(cfg, seed):
+    import mpaso
+    from mpaso.initial import ocean_state, sw_state
+    from mpaso.setup import fct_statics
+    t0 = time.time()
+    mesh = mpaso.Mesh.icosa(cfg["level"])
+    fct = fct_statics(mesh, cfg["L"])
+    if cfg["app"] == "sw":
+        state = sw_state(mesh, seed, cfg["L"], cfg["T"])
+    else:
+        state = ocean_state(mesh, seed, cfg["L"], cfg["T"])
+    log(f"workload built in {time.time() - t0:.1f}s: {mesh.nCells} cells")
+    return mesh, fct, state
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4)
+                          if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def gpu_arm(args, cfg):
+    import numpy as np
+    import torch
+
+    import mpaso.gpu as G
+    from mpaso.perfmodel import Dims, ocean_kernels, per_step, sw_kernels
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    mesh, fct, state = build_workload(cfg, seed=1000 + rank)
+    dm = G.DeviceMesh(mesh, fct=fct, device=local)
+    app = G.APP_SW if cfg["app"] == "sw" else G.APP_OCEAN
+    st = G.State(dm, app=app, nlev=cfg["L"], ntr=cfg["T"], fct=cfg["fct"], hmix=cfg["hmix"],
+                 kappa=cfg["kappa"], nu=cfg["nu"])
+    if app == G.APP_SW:
+        h, u, tr = state
+        fields = ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr))
+    else:
+        h, hE, u, tr = state
+        fields = ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr), (G.FIELD_LAYER_THICKNESS_EDGE, hE))
+    for f, a in fields:
+        st.set(f, a)
+    dt, K, W = cfg["dt"], args.steps, args.warmup
+    ext = torch.cuda.ExternalStream(st.stream())
+    st.step_graph(dt, W)
+    st.sync()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    time.sleep(0.3)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    st.step_graph(dt, K)
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    barrier()
+    clocks = sampler.stop()
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    units_rank = mesh.nCells * cfg["L"]
+    value = world * units_rank * K / (ms_max * 1e-3)
+
+    # ---- per-kernel timing (live, CUDA events between launches) and roofline
+    prof = st.profile(dt, min(K, 20))
+    dims = Dims.of(mesh, cfg["L"], cfg["T"], fct)
+    model = (sw_kernels(dims, cfg["fct"], cfg["hmix"], cfg["nu"] != 0.0) if app == G.APP_SW
+             else ocean_kernels(dims, cfg["fct"], cfg["hmix"]))
+    step_bytes, step_fp64 = per_step(model)
+    top = max(prof, key=prof.get)
+    prof_total = sum(prof.values())
+    peak, peak_kind = measured_peaks()
+    fp64_peak = G.probe_fp64(local)
+    kb, kf = model[top]
+    achieved = kb / (prof[top] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"{top}_{args.config}.txt")
+    if os.path.exists(tfile):
+        for line in open(tfile):
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": top,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": int(kb),
+                "kernel_time_share": round(prof[top] / prof_total, 3)}
+    fp64 = {"achieved_dfma_per_s": kf / (prof[top] * 1e-3), "peak_dfma_per_s": fp64_peak,
+            "frac": round(kf / (prof[top] * 1e-3) / fp64_peak, 4), "kernel": top,
+            "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / fp64_peak, 4),
+            "note": "FP64 instructions per launch from mpaso/perfmodel.py / measured launch time, "
+                    "against the live DFMA issue rate of mpaso_probe_fp64"}
+    step_hbm = {"algorithmic_bytes_per_step": int(step_bytes),
+                "achieved_gbs": round(step_bytes / (ms_max * 1e-3 / K) / 1e9, 1),
+                "frac": round(step_bytes / (ms_max * 1e-3 / K) / 1e9 / peak, 4),
+                "bytes_per_cell_update": round(step_bytes / units_rank, 1)}
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    Ke = min(K, 50)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()  # noqa: E731
+    if app == G.APP_SW:
+        hp, up, tp = pin(h), pin(u), pin(tr)
+        nbytes = (hp.numel() + up.numel() + tp.numel()) * 8
+        st.step_host(dt, 1, hp, up, tp)  # warm the staging path
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(ext)
+        for _ in range(Ke):
+            st.step_host(dt, 1, hp, up, tp)
+        a1.record(ext)
+        a1.synchronize()
+        e2e_ms = a0.elapsed_time(a1)
+    else:
+        tp = pin(tr)
+        nbytes = tp.numel() * 8
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(ext)
+        for _ in range(Ke):
+            st.set(G.FIELD_TRACERS, tp)
+            st.step_graph(dt, 1)
+            st.get(G.FIELD_TRACERS, tp.numpy())
+        a1.record(ext)
+        a1.synchronize()
+        e2e_ms = a0.elapsed_time(a1)
+    t = torch.tensor([e2e_ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e = {"value": world * units_rank * Ke / (float(t.item()) * 1e-3), "unit": "cell-updates/s",
+           "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
+           "path": "mpaso_rk4_step_host (C ABI, pinned host buffers, copy in -> 1 step -> copy out)"
+           if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)"}
+
+    out = None
+    if rank == 0:
+        cpu = cpu_baseline(cfg, mesh, fct, state) if (world == 1 and not args.no_cpu_baseline) else None
+        working_set = dm.device_bytes() + st.device_bytes()
+        out = {
+            "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded smooth fields on generated mesh)",
+            "config": {"workload": cfg["workload"], "config": args.config, "cells": mesh.nCells,
+                       "edges": mesh.nEdges, "vertices": mesh.nVertices, "levels": cfg["L"],
+                       "tracers": cfg["T"], "dt_s": dt, "fct": cfg["fct"], "del2_tracer": cfg["kappa"],
+                       "del2_momentum": cfg["nu"], "parallelism": f"replicas x{world}",
+                       "l2": f"device working set {working_set / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2 "
+                             "(no flush)", "timing": "CUDA events on the state stream, graph-replayed steps"},
+            "roofline": roofline, "fp64": fp64, "step_hbm": step_hbm,
+            "kernels_ms_per_launch": {k: round(v, 5) for k, v in prof.items()},
+            "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu,
+            "gpu_launches": st.launches_per_step() * K,
+        }
+    st.close()
+    dm.close()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def cpu_baseline(cfg, mesh, fct, state, budget_s=12.0):
+    """The oracle's C restatement of the reference tasks, one core, a bounded
+    number of full RK4 steps on the same mesh and state."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    O = Oracle("restatement")
+    st = O.static(mesh, fct)
+    c = O.config(cfg["L"], cfg["T"], fct=cfg["fct"], hmix=cfg["hmix"], kappa=cfg["kappa"], nu=cfg["nu"])
+    om = O.mesh(mesh)
+    run = ((lambda n: O.sw_run(om, st, c, cfg["dt"], n, *state)) if cfg["app"] == "sw"
+           else (lambda n: O.ocean_run(om, st, c, cfg["dt"], n, state[0], state[1], state[2], state[3])))
+    t0 = time.perf_counter()
+    run(1)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(50, int(budget_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    run(n)
+    el = time.perf_counter() - t0
+    return {"value": mesh.nCells * cfg["L"] * n / el, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{n} RK4 steps of the same {mesh.nCells}-cell workload, oracle C restatement "
+                      f"(bit-identical to the reference tasks), gcc -O3, one thread"}
+
+
+# ---------------------------------------------------------------- reference arm
+def _ref_worker(args):
+    cfg_name, steps, warmup, seed, kind, barrier = args
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    cfg = CONFIGS[cfg_name]
+    mesh, _, state = build_workload(cfg, seed)
+    O = Oracle("restatement") if kind == "port" else Oracle("ref", cfg["L"], cfg["T"])
+    fct = O.fct_statics(mesh, cfg["L"], cfg=O.config(cfg["L"], cfg["T"]))
+    st, om = O.static(mesh, fct), O.mesh(mesh)
+    c = O.config(cfg["L"], cfg["T"], fct=cfg["fct"], hmix=cfg["hmix"], kappa=cfg["kappa"], nu=cfg["nu"])
+
+    def run(n):
+        if cfg["app"] == "sw":
+            return O.sw_run(om, st, c, cfg["dt"], n, *state)
+        return O.ocean_run(om, st, c, cfg["dt"], n, *state)
+    if warmup:
+        run(warmup)
+    barrier.wait()  # every process built and warmed up; the parent starts its clock
+    t0 = time.perf_counter()
+    run(steps)
+    return mesh.nCells * cfg["L"], time.perf_counter() - t0
+
+
+def reference_arm(args, cfg):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    kind = "port"
+    ref_lib = os.path.join(ROOT, "oracle", "_ref", f"libref_L{cfg['L']}_T{cfg['T']}.so")
+    if os.path.exists(ref_lib):
+        try:
+            import ctypes
+            ctypes.CDLL(ref_lib)
+            kind = "reference"
+        except OSError:
+            kind = "port"
+    steps = max(1, min(args.steps, args.ref_max_steps))
+    warm = min(args.warmup, 1)
+    cores = args.ref_procs or (os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    barrier = mgr.Barrier(cores + 1)
+    with ctx.Pool(cores) as pool:
+        res = pool.map_async(_ref_worker, [(args.config, steps, warm, 2000 + i, kind, barrier)
+                                           for i in range(cores)])
+        barrier.wait()
+        t0 = time.perf_counter()
+        out = res.get()
+        wall = time.perf_counter() - t0
+    units = [u for u, _ in out]
+    times = [t for _, t in out]
+    value = sum(units) * steps / max(max(times), 1e-9)
+    desc = (f"{cores} processes x {steps} RK4 steps of the {cfg['workload']} workload, "
+            f"{'reference task sources via the oracle shim' if kind == 'reference' else 'oracle C restatement of the reference tasks'}, "
+            "gcc -O3, one thread each")
+    return {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": steps,
+            "warmup": warm, "ms_per_step": max(times) / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded smooth fields on generated mesh)", "impl": "reference",
+            "config": {"workload": cfg["workload"], "config": args.config, "wall_s": round(wall, 2)},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": kind,
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="sw_l7", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-max-steps", type=int, default=4, help="reference arm: steps timed per process")
+    ap.add_argument("--ref-procs", type=int, default=0, help="reference arm: processes (0 = all cores)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        log("note: fewer than 3 warm-up steps")
+    cfg = CONFIGS[args.config]
+    out = reference_arm(args, cfg) if args.impl == "reference" else gpu_arm(args, cfg)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -195,9 +195,19 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
                         double *tracers);
 int mpaso_state_sync(mpaso_state s);
 int mpaso_state_stream(mpaso_state s, void **stream);
+/* Per-kernel timing: runs nsteps steps (not from a graph) with CUDA events
+ * around every launch on the state's stream and returns, for each of the
+ * *nkinds kernel kinds of a stage (at most 8), the mean duration of one
+ * launch in ms.  names (optional) receives a ','-separated list of kinds. */
+int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per_launch,
+                        int32_t *nkinds, char *names, int32_t names_len);
 /* Kernel launches issued per RK4 step by mpaso_rk4_step. */
 int mpaso_state_launches_per_step(mpaso_state s, int32_t *n);
 int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
+
+/* FP64 ceiling of `device`: DFMA lane-operations per second issued by a
+ * compute-only probe kernel (GB300 runs FP64 at a small fraction of FP32). */
+int mpaso_probe_fp64(int device, double *dfma_per_s);
 
 /* Device / runtime queries (no GPU needed: report 0 devices). */
 int mpaso_device_count(int32_t *n);

@@ -75,6 +75,45 @@ const char *mpaso_genmesh_names(void);
 
 void mpaso_genmesh_free(mpaso_genmesh m);
 
+/* ------------------------------------------------------------------------
+ * FCT / del2 static coefficients (host), the setup of
+ * apps/ocean/tasks/init_functions.cc:18-447 as apps/ocean/initialize.cc:
+ * 391-400 runs it: maxLevelEdgeTop, meshScalingDel2, edgeSignOnCell,
+ * derivTwo (second-derivative least-squares fit on the tangent plane),
+ * advCellsForEdge / advCoef / advCoef_3rd, highOrderAdvMask.
+ * On the sphere the results equal the reference's bit for bit.  The
+ * reference has no planar branch (init_functions.cc:198-200, 282-283,
+ * 321-322 are empty); on_sphere = 0 fits the same polynomial in plane
+ * coordinates with minimum-image offsets on a periodic domain.
+ * Connectivity is FleCSI's 0-based CRS in file order (as in mpaso_mesh_desc).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int64_t nCells, nEdges, nVertices;
+  const int64_t *c2e_off, *c2c_off, *e2v_off;
+  const int32_t *c2e, *c2c, *e2v;
+  const double *dcEdge, *dvEdge;
+  const double *xCell, *yCell, *zCell, *xVertex, *yVertex, *zVertex;
+  const double *meshDensity;
+  int32_t on_sphere;
+  double Lx, Ly;               /* planar periodic extents (0 = not periodic) */
+  int32_t nlev;
+  const int32_t *maxLevelCell; /* [nC] */
+  const int32_t *boundaryCell; /* [nC][nlev]; NULL = no boundary cells */
+} mpaso_fct_setup_in;
+
+typedef struct {
+  int32_t *maxLevelEdgeTop;  /* [nE] */
+  double *meshScalingDel2;   /* [nE] */
+  double *edgeSignOnCell;    /* [nC][8] */
+  double *derivTwo;          /* [nE][16][2] */
+  int32_t *nAdvCellsForEdge; /* [nE] */
+  int32_t *advCellsForEdge;  /* [nE][16] */
+  int32_t *highOrderAdvMask; /* [nE][nlev] */
+  double *advCoef, *advCoef_3rd; /* [nE][16] */
+} mpaso_fct_setup_out;
+
+int mpaso_fct_setup(const mpaso_fct_setup_in *in, mpaso_fct_setup_out *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,9 +99,13 @@ Stage ocean_stage(SwState &s, int rk, double dt) {
 template <int T> void ocean_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
+  cudaEvent_t *ev = s.prof_events;
   k_oc_edges<T><<<blocks_for((int64_t)m.nE * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
   k_oc_cells<T><<<blocks_for((int64_t)m.nC * L, TPB), TPB, 0, st>>>(m, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
   k_oc_final<T><<<blocks_for((int64_t)m.nC * L, TPB), TPB, 0, st>>>(m, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
 }  // namespace
@@ -130,23 +134,25 @@ void ocean_prepare(SwState &s, double dt, cudaStream_t st) {
   }
 }
 
+void ocean_one_stage(SwState &s, int rk, double dt, cudaStream_t st) {
+  const Stage S = ocean_stage(s, rk, dt);
+  switch (s.T) {
+    case 1: ocean_stage_T<1>(s, S, st); break;
+    case 2: ocean_stage_T<2>(s, S, st); break;
+    case 3: ocean_stage_T<3>(s, S, st); break;
+    case 4: ocean_stage_T<4>(s, S, st); break;
+    case 5: ocean_stage_T<5>(s, S, st); break;
+    case 6: ocean_stage_T<6>(s, S, st); break;
+    case 7: ocean_stage_T<7>(s, S, st); break;
+    case 8: ocean_stage_T<8>(s, S, st); break;
+    default: fail(MPASO_ERR_ARG, "ocean app needs 1..8 tracers");
+  }
+}
+
 void ocean_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
   ocean_prepare(s, dt, st);
   for (int n = 0; n < nsteps; ++n)
-    for (int rk = 0; rk < 4; ++rk) {
-      const Stage S = ocean_stage(s, rk, dt);
-      switch (s.T) {
-        case 1: ocean_stage_T<1>(s, S, st); break;
-        case 2: ocean_stage_T<2>(s, S, st); break;
-        case 3: ocean_stage_T<3>(s, S, st); break;
-        case 4: ocean_stage_T<4>(s, S, st); break;
-        case 5: ocean_stage_T<5>(s, S, st); break;
-        case 6: ocean_stage_T<6>(s, S, st); break;
-        case 7: ocean_stage_T<7>(s, S, st); break;
-        case 8: ocean_stage_T<8>(s, S, st); break;
-        default: fail(MPASO_ERR_ARG, "ocean app needs 1..8 tracers");
-      }
-    }
+    for (int rk = 0; rk < 4; ++rk) ocean_one_stage(s, rk, dt, st);
   MPASO_CUDA(cudaGetLastError());
 }
 

@@ -287,9 +287,13 @@ Stage make_stage(SwState &s, int rk, double dt) {
 template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
+  cudaEvent_t *ev = s.prof_events;
   k_sw_edge_pre<T><<<blocks_for((int64_t)m.nE * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
   k_sw_tend<T><<<blocks_for(((int64_t)m.nE + m.nC) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
   k_sw_final<T><<<blocks_for(((int64_t)m.nC + m.nV) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
 void launch_stage(SwState &s, const Stage &S, cudaStream_t st) {
@@ -329,6 +333,7 @@ void sw_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
 void ocean_create(SwState &s);
 void ocean_steps(SwState &s, double dt, int nsteps, cudaStream_t st);
 void ocean_prepare(SwState &s, double dt, cudaStream_t st);
+void ocean_one_stage(SwState &s, int rk, double dt, cudaStream_t st);
 int ocean_launches_per_step(const SwState &s);
 
 void sw_create(SwState &s) {
@@ -528,6 +533,54 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
   if (!rc) rc = mpaso_state_get(s, MPASO_FIELD_U, u);
   if (!rc && tracers && s->s.T > 0) rc = mpaso_state_get(s, MPASO_FIELD_TRACERS, tracers);
   return rc;
+}
+
+int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per_launch,
+                        int32_t *nkinds, char *names, int32_t names_len) {
+  return guarded("mpaso_state_profile", [&] {
+    require(s && ms_per_launch && nkinds && nsteps > 0, MPASO_ERR_ARG, "bad argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    const bool oc = S.p.app == MPASO_APP_OCEAN;
+    const char *kinds = oc ? "oc_edges,oc_cells,oc_final" : "sw_edge_pre,sw_tend,sw_final";
+    const int nk = 3;
+    if (oc)
+      ocean_prepare(S, dt, S.stream);
+    else
+      ensure_diag(S, S.stream);
+    std::vector<cudaEvent_t> ev(nk + 1);
+    for (auto &e : ev) MPASO_CUDA(cudaEventCreate(&e));
+    double acc[8] = {0};
+    S.prof_events = ev.data() + 1;
+    try {
+      for (int n = 0; n < nsteps; ++n)
+        for (int rk = 0; rk < 4; ++rk) {
+          MPASO_CUDA(cudaEventRecord(ev[0], S.stream));
+          if (oc)
+            ocean_one_stage(S, rk, dt, S.stream);
+          else
+            launch_stage(S, make_stage(S, rk, dt), S.stream);
+          MPASO_CUDA(cudaEventSynchronize(ev[nk]));
+          for (int k = 0; k < nk; ++k) {
+            float ms = 0.f;
+            MPASO_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            acc[k] += ms;
+          }
+        }
+    } catch (...) {
+      S.prof_events = nullptr;
+      for (auto &e : ev) cudaEventDestroy(e);
+      throw;
+    }
+    S.prof_events = nullptr;
+    for (auto &e : ev) MPASO_CUDA(cudaEventDestroy(e));
+    for (int k = 0; k < nk; ++k) ms_per_launch[k] = acc[k] / (4.0 * nsteps);
+    *nkinds = nk;
+    if (names && names_len > 0) {
+      std::strncpy(names, kinds, (size_t)names_len - 1);
+      names[names_len - 1] = 0;
+    }
+  });
 }
 
 int mpaso_state_sync(mpaso_state s) {

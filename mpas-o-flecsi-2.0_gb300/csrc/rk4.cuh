@@ -69,6 +69,8 @@ struct SwState {
   double prep_dt = 0.0;     // ocean: dt of the cached F / 1/hProv (0 = stale)
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0.0;
+  // optional per-launch timing: events recorded after every kernel of a stage
+  cudaEvent_t *prof_events = nullptr;
   ~SwState();
 };
 

@@ -60,6 +60,13 @@ def _ptr(a):
     raise TypeError(f"unsupported array type {type(a)}")
 
 
+def probe_fp64(device=0):
+    """DFMA lane-operations per second of the device (live FP64 ceiling)."""
+    v = ctypes.c_double()
+    check(lib().mpaso_probe_fp64(int(device), ctypes.byref(v)))
+    return v.value
+
+
 def device_count():
     n = ctypes.c_int32()
     check(lib().mpaso_device_count(ctypes.byref(n)))
@@ -227,6 +234,15 @@ class State:
         s = ctypes.c_void_p()
         check(lib().mpaso_state_stream(self._h, ctypes.byref(s)))
         return s.value
+
+    def profile(self, dt, nsteps):
+        """Mean ms per launch of each stage kernel kind: dict name -> ms."""
+        ms = (ctypes.c_double * 8)()
+        n = ctypes.c_int32()
+        names = ctypes.create_string_buffer(256)
+        check(lib().mpaso_state_profile(self._h, ctypes.c_double(dt), int(nsteps), ms, ctypes.byref(n),
+                                        names, 256))
+        return dict(zip(names.value.decode().split(","), list(ms)[:n.value]))
 
     def launches_per_step(self):
         n = ctypes.c_int32()

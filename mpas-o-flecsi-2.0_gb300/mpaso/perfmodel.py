@@ -1,0 +1,117 @@
+"""Algorithmic traffic and FP64 work of the fused RK4 kernels.
+
+Bytes: every array a launch touches counted once (reads + writes), at its
+real size on the mesh (8 B per double, 4 B per index), the compulsory traffic
+of the dataflow -- repeated gathers of a neighbour's value are not counted
+again.  FP64 work: DADD / DMUL / DFMA instructions per launch (a division by
+rcp_nr is 5 instructions plus one multiply); min/max/select/sign work runs on
+the integer pipe and is not counted.
+
+One cell-update = one cell x one level advanced by one full RK4 step.
+"""
+from dataclasses import dataclass
+
+
+@dataclass
+class Dims:
+    nC: int
+    nE: int
+    nV: int
+    L: int
+    T: int
+    maxEoE: int  # edgesOnEdge slots (padded)
+    maxAdv: int  # advection cells per edge (padded)
+    avgEoC: float  # mean edges per cell
+
+    @classmethod
+    def of(cls, mesh, L, T, fct_statics=None):
+        f = mesh.fields
+        maxEoE = int(f["nEdgesOnEdge"].max())
+        maxAdv = int(fct_statics["nAdvCellsForEdge"].max()) if fct_statics is not None else 1
+        return cls(mesh.nCells, mesh.nEdges, mesh.nVertices, L, T, maxEoE, maxAdv,
+                   float(f["nEdgesOnCell"].mean()))
+
+
+def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
+    """Per-launch (bytes, fp64 instructions) of the three sw stage kernels,
+    averaged over the four RK stages."""
+    nC, nE, nV, L, T = d.nC, d.nE, d.nV, d.L, d.T
+    Ne, Na, Nc = d.maxEoE, d.maxAdv, d.avgEoC
+    cl, el, vl = nC * L, nE * L, nV * L
+    slot_c = Nc * nC  # ragged cell slots
+    # ---- K1 edge pre-pass
+    b1 = 8 * nE * 2 + 8 * cl + 8 * el + 8 * vl + 24 * el
+    f1 = 6 * el
+    if T:
+        b1 += 8 * cl * T + 8 * nE
+        f1 += el
+        if fct:
+            b1 += 12 * Na * nE + 4 * el + 16 * el * T
+            f1 += el * T * (Na + 3)
+        else:
+            b1 += 8 * el * T
+            f1 += 2 * el * T
+        if hmix:
+            b1 += 8 * nE + 8 * el * T
+            f1 += el * (1 + 2 * T)
+    # ---- K2 edges + cells
+    b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * nE + 8 * cl + 8 * nE
+    b2 += 8 * el + 16 * el + 8 * el * 0.75
+    f2 = el * (2 * Ne + 8 + 1.75)
+    if visc:
+        b2 += 8 * cl + 8 * vl + 16 * nE
+        f2 += 6 * el
+    b2 += 4 * nC + 12 * slot_c + 8 * nC + 8 * cl + 16 * cl + 8 * cl * 0.75
+    f2 += cl * (Nc + 1 + 1.75)
+    if T:
+        b2 += 8 * slot_c
+        if fct:
+            b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
+            f2 += cl * (7 + T * (3 * Nc + 26))
+        else:
+            b2 += 8 * el * T + 8 * cl * T
+            f2 += cl * T * (Nc + 1)
+    # ---- K3 cells + vertices
+    b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl  # diag: kw, u_next, invArea, ke
+    f3 = cl * (2 * Nc + 1)
+    if visc:
+        b3 += 8 * slot_c + 8 * cl
+        f3 += cl * (Nc + 1)
+    if T:
+        b3 += 4 * nC + 12 * slot_c + 8 * nE + 8 * cl * 2 + 8 * cl * T * 2 + 16 * cl * T + 8 * cl * T * 0.75
+        if fct:
+            b3 += 8 * el * T + 16 * cl * T
+        if hmix:
+            b3 += 8 * el * T
+        f3 += cl * (5 + T * (3 * Nc + 4))
+    b3 += 8 * nV * (3 + 1.5 + 3 + 1.5 + 3) + 8 * vl + 16 * vl
+    f3 += vl * 14
+    return {"sw_edge_pre": (b1, f1), "sw_tend": (b2, f2), "sw_final": (b3, f3)}
+
+
+def ocean_kernels(d: Dims, fct=True, hmix=True):
+    """Per-launch (bytes, fp64 instructions) of the three ocean stage kernels."""
+    nC, nE, L, T = d.nC, d.nE, d.L, d.T
+    Na, Nc = d.maxAdv, d.avgEoC
+    cl, el = nC * L, nE * L
+    slot_c = Nc * nC
+    b1 = 8 * nE + 8 * el + 8 * cl * T + 8 * nE + 8 * el  # coe, F, tr_in, dv, hE
+    f1 = el
+    if fct:
+        b1 += 12 * Na * nE + 4 * el + 16 * el * T
+        f1 += el * T * (Na + 3)
+    if hmix:
+        b1 += 8 * nE + 8 * el * T
+        f1 += el * (1 + 2 * T)
+    b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
+    b2 += 16 * el * T + 24 * cl * T
+    f2 = cl * (1 + T * (3 * Nc + 26))
+    b3 = 4 * nC + 12 * slot_c + 8 * nC + 8 * nE + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
+    b3 += 8 * el * T * (int(fct) + int(hmix))
+    f3 = cl * T * (3 * Nc + 3)
+    return {"oc_edges": (b1, f1), "oc_cells": (b2, f2), "oc_final": (b3, f3)}
+
+
+def per_step(kernels):
+    """Bytes and FP64 instructions of one RK4 step (four stages)."""
+    return (4 * sum(b for b, _ in kernels.values()), 4 * sum(f for _, f in kernels.values()))
