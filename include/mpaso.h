@@ -99,6 +99,20 @@ int mpaso_sw_compute_solve_diagnostics(mpaso_mesh m, int32_t nlev, const double 
 int mpaso_sw_compute_tend(mpaso_mesh m, int32_t nlev, const double *h_edge, const double *h,
                           const double *u, const double *ke, const double *pv_edge,
                           double *tend_h, double *tend_u, void *stream);
+/* Allocation-free compute_tend (no counterpart in the reference).  Same
+ * arguments and results as mpaso_sw_compute_tend, for callers that must not
+ * allocate device memory during the call (a task inside a runtime that pools
+ * all device memory, or code that cannot afford cudaMalloc's device-wide
+ * synchronisation).  All seven arrays must be device memory.  Arguments are
+ * staged through one static 32 MiB device array instead of allocated scratch,
+ * which limits the mesh to (4 nEdges + 3 nCells) * nlev <= 4,194,304 doubles
+ * (larger meshes get MPASO_ERR_ARG).  The first call on a device looks up that
+ * array's address (cudaGetSymbolAddress): make it before any stream capture.
+ * Every call shares the array, so calls whose GPU work overlaps race. */
+int mpaso_sw_compute_tend_noalloc(mpaso_mesh m, int32_t nlev, const double *h_edge,
+                                  const double *h, const double *u, const double *ke,
+                                  const double *pv_edge, double *tend_h, double *tend_u,
+                                  void *stream);
 /* apps/sw/tasks/solve.cc:237-270 */
 int mpaso_sw_compute_scalar_tend(mpaso_mesh m, int32_t nlev, int32_t ntr, const double *h_edge,
                                  const double *u, const double *tracers, double *tracer_tend,

@@ -451,6 +451,16 @@ struct Flat {
 };
 
 }  // namespace
+
+// Launches the compute_tend kernel on arrays already in the context's
+// numbering (used by the allocation-free entry point in noalloc.cu).
+void launch_task_sw_tend(const DMesh &d, int L, double g, const double *h_edge, const double *h,
+                         const double *u, const double *ke, const double *pv_edge, double *tend_h,
+                         double *tend_u, cudaStream_t s) {
+  const int64_t n = ((int64_t)d.nE + d.nC) * L;
+  k_sw_tend<<<blocks_for(n, TPB), TPB, 0, s>>>(d, L, g, h_edge, h, u, ke, pv_edge, tend_h, tend_u);
+}
+
 }  // namespace mpaso
 
 using namespace mpaso;
