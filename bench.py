@@ -290,6 +290,142 @@ def cpu_baseline(cfg, mesh, fct, state, budget_s=12.0):
                       f"(bit-identical to the reference tasks), gcc -O3, one thread"}
 
 
+# ---------------------------------------------------------------- adjoint (cfg3)
+def adjoint_arm(args):
+    """Gradient of J = 1/2 <area (h_N - h_target)^2> / sum(area) w.r.t. (h0, u0):
+    level-6 sphere, 500 RK4 steps of dt = 90 s, checkpoints every 25 steps."""
+    import numpy as np
+    import torch
+
+    import mpaso
+    import mpaso.gpu as G
+    from mpaso.initial import sw_state
+    N, K, dt, level = args.adj_steps, args.adj_ckpt, 90.0, 6
+    mesh = mpaso.Mesh.icosa(level)
+    h0, u0, _ = sw_state(mesh, 1234, 1, 1)
+    ht, _, _ = sw_state(mesh, 4321, 1, 1)
+    area = mesh.fields["areaCell"][:, None]
+    w = area / area.sum()
+    dm = G.DeviceMesh(mesh)
+    st = G.State(dm, nlev=1, ntr=0)
+    ext = torch.cuda.ExternalStream(st.stream())
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        fn()
+        e1.record(ext)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    def loss(h, u):
+        st.set(G.FIELD_H, h)
+        st.set(G.FIELD_U, u)
+        st.step(dt, N)
+        hN = st.get(G.FIELD_H)
+        return 0.5 * float((w * (hN - ht) ** 2).sum()), hN
+
+    for _ in range(2):  # warm-up
+        st.set(G.FIELD_H, h0), st.set(G.FIELD_U, u0)
+        st.forward(dt, min(N, 50), K)
+    st.set(G.FIELD_H, h0), st.set(G.FIELD_U, u0)
+    t_plain = timed(lambda: st.step(dt, N))
+    st.set(G.FIELD_H, h0), st.set(G.FIELD_U, u0)
+    t_fwd = timed(lambda: st.forward(dt, N, K))
+    hN = st.get(G.FIELD_H)
+    gh_N = w * (hN - ht)
+    out = {}
+    t_vjp = timed(lambda: out.update(g=st.vjp(gh_N, np.zeros_like(u0))))
+    gh, gu = out["g"]
+    rng = np.random.default_rng(7)
+    errs = []
+    for _ in range(args.adj_dirs):
+        dh = rng.standard_normal(h0.shape) * 0.1
+        du = rng.standard_normal(u0.shape) * 1e-3
+        eps = 1.0
+        jp, _ = loss(h0 + eps * dh, u0 + eps * du)
+        jm, _ = loss(h0 - eps * dh, u0 - eps * du)
+        fd = (jp - jm) / (2 * eps)
+        ad = float((gh * dh).sum() + (gu * du).sum())
+        errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+    mem = dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes()
+    return {"metric": "adjoint/forward time ratio (sw RK4, level-6 sphere)",
+            "value": t_vjp / t_fwd, "unit": "ratio", "higher_is_better": False, "n_gpus": 1,
+            "steps": N, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
+            "config": {"workload": f"sphere-level{level} sw RK4, {N} steps, dt={dt}s, checkpoint every {K}",
+                       "cells": mesh.nCells, "edges": mesh.nEdges,
+                       "loss": "0.5 * sum(area (h_N - h_target)^2) / sum(area)"},
+            "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp,
+            "vjp_over_plain_forward": t_vjp / t_plain,
+            "fd_check": {"directions": args.adj_dirs, "max_rel_err": max(errs),
+                         "median_rel_err": float(np.median(errs))},
+            "peak_device_bytes": int(mem)}
+
+
+# ---------------------------------------------------------------- ensemble (cfg4)
+def ensemble_arm(args):
+    """256 uneven members (192 periodic hex meshes, 64 spheres) advanced as one
+    union, against the same members advanced one at a time."""
+    import numpy as np
+    import torch
+
+    import mpaso.gpu as G
+    from mpaso.ensemble import build
+    from mpaso.initial import sw_state
+    rng = np.random.default_rng(2024)
+    sides = [32, 48, 64, 96, 128, 192, 256]
+    specs = [("hex", int(s), int(s), 10e3, 1e-4) for s in rng.choice(sides, args.ens_planar)]
+    specs += [("icosa", int(l)) for l in rng.choice([5, 6], args.ens_sphere)]
+    t0 = time.time()
+    u, fct, offs, members, mfct = build(specs, nlev=1, return_member_fct=True)
+    states = [sw_state(m, 5000 + i, 1, 1) for i, m in enumerate(members)]
+    log(f"ensemble built in {time.time() - t0:.1f}s: {len(members)} members, {u.nCells} cells")
+    opts = dict(fct=True, hmix=True, kappa=1e3, nu=1e3)
+    dt, K, W = 30.0, args.steps, args.warmup
+    dm = G.DeviceMesh(u, fct=fct, reorder=False)
+    st = G.State(dm, nlev=1, ntr=1, **opts)
+    for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
+        st.set(f, np.concatenate([s[k] for s in states]))
+    ext = torch.cuda.ExternalStream(st.stream())
+    st.step_graph(dt, W)
+    st.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    st.step_graph(dt, K)
+    e1.record(ext)
+    e1.synchronize()
+    t_batch = e0.elapsed_time(e1) * 1e-3
+    # one member at a time: its own context and graph, members advanced in turn
+    singles = []
+    for i, m in enumerate(members):
+        d = G.DeviceMesh(m, fct=mfct[i], reorder=False)
+        s = G.State(d, nlev=1, ntr=1, **opts)
+        for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
+            s.set(f, states[i][k])
+        s.step_graph(dt, W)
+        singles.append((d, s))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for d, s in singles:
+        s.step_graph(dt, K)
+    for d, s in singles:
+        s.sync()
+    t_single = time.perf_counter() - t1
+    n = len(members)
+    return {"metric": "ensemble members*steps/s (one graph-captured launch sequence vs one at a time)",
+            "value": n * K / t_batch, "unit": "member-steps/s", "higher_is_better": True, "n_gpus": 1,
+            "steps": K, "warmup": W, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
+            "config": {"workload": f"{args.ens_planar} periodic hex (sides 32..256) + {args.ens_sphere} "
+                                   f"sphere (level 5/6) members, sw + FCT tracer + del2, dt={dt}s",
+                       "cells": int(u.nCells), "edges": int(u.nEdges), "members": n},
+            "cell_updates_per_s": u.nCells * K / t_batch,
+            "one_at_a_time": {"value": n * K / t_single, "unit": "member-steps/s",
+                              "cell_updates_per_s": u.nCells * K / t_single},
+            "speedup_vs_one_at_a_time": t_single / t_batch,
+            "gpu_launches": st.launches_per_step() * K}
+
+
 # ---------------------------------------------------------------- reference arm
 def _ref_worker(args):
     cfg_name, steps, warmup, seed, kind, barrier = args
@@ -365,15 +501,25 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="sw_l7", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="sw_l7", choices=sorted(CONFIGS) + ["adjoint_l6", "ensemble"])
+    ap.add_argument("--adj-steps", type=int, default=500)
+    ap.add_argument("--adj-ckpt", type=int, default=25)
+    ap.add_argument("--adj-dirs", type=int, default=32)
+    ap.add_argument("--ens-planar", type=int, default=192)
+    ap.add_argument("--ens-sphere", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-max-steps", type=int, default=4, help="reference arm: steps timed per process")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm: processes (0 = all cores)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         log("note: fewer than 3 warm-up steps")
-    cfg = CONFIGS[args.config]
-    out = reference_arm(args, cfg) if args.impl == "reference" else gpu_arm(args, cfg)
+    if args.config == "adjoint_l6":
+        out = adjoint_arm(args)
+    elif args.config == "ensemble":
+        out = ensemble_arm(args)
+    else:
+        cfg = CONFIGS[args.config]
+        out = reference_arm(args, cfg) if args.impl == "reference" else gpu_arm(args, cfg)
     if out is not None:
         print(json.dumps(out), flush=True)
 

@@ -64,6 +64,10 @@ struct DMesh {
   const int *eov;             // [3][nV] edges(v): ascending reference ids (transposed e2v)
   const double *eovSign;      // [3][nV] -1: v is vertices(e)[0], +1: vertices(e)[1]
   const double *areaTriangle, *invAreaTriangle, *fVertex;
+  // ---- reverse connectivity for the adjoint (gathers instead of scatters) ----
+  const double *woeT;         // [maxEoE][nE] weight of e in the stencil of eoe[j][e] (0 in pads)
+  const int *vocR;            // [maxEoC][nC] vertices of c (pads repeat slot 0)
+  const double *kiteR;        // [maxEoC][nC] kite of c at vocR[j][c] (0 in pads)
 };
 
 // Host-side mesh context.

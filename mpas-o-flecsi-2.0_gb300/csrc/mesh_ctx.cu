@@ -299,6 +299,33 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d) {
   A.add(cov, &m.cov), A.add(kite, &m.kite), A.add(eov, &m.eov), A.add(eovSign, &m.eovSign);
   A.add(aT, &m.areaTriangle), A.add(iaT, &m.invAreaTriangle), A.add(fV, &m.fVertex);
 
+  // ---- reverse connectivity (adjoint): transposed TRiSK weights, cell -> (vertex, kite) ----
+  // e' in edgesOnEdge(e) <=> e in edgesOnEdge(e') (both share a cell), so the
+  // transposed stencil of e is its own stencil with the partner's weight.
+  std::vector<double> woeT((size_t)std::max(maxEoE, 1) * nE, 0.0);
+  for (int64_t k = 0; k < nE; ++k)
+    for (int j = 0; j < nEoE[k]; ++j) {
+      const int eo = eoe[(size_t)j * nE + k];
+      int p = 0;
+      while (p < nEoE[eo] && eoe[(size_t)p * nE + eo] != (int)k) ++p;
+      require(p < nEoE[eo], MPASO_ERR_MESH, "edgesOnEdge is not symmetric");
+      woeT[(size_t)j * nE + k] = woe[(size_t)p * nE + eo];
+    }
+  std::vector<int> vocR((size_t)maxEoC * nC, 0);
+  std::vector<double> kiteR((size_t)maxEoC * nC, 0.0);
+  std::vector<int> fillc(nC, 0);
+  for (int64_t v = 0; v < nV; ++v)
+    for (int j = 0; j < kVertexDegree; ++j) {
+      const int c = cov[(size_t)j * nV + v];
+      require(fillc[c] < maxEoC, MPASO_ERR_MESH, "cell with more vertices than edges");
+      vocR[(size_t)fillc[c] * nC + c] = (int)v;
+      kiteR[(size_t)fillc[c] * nC + c] = kite[(size_t)j * nV + v];
+      fillc[c]++;
+    }
+  for (int64_t c = 0; c < nC; ++c)
+    for (int j = fillc[c]; j < maxEoC; ++j) vocR[(size_t)j * nC + c] = vocR[c];
+  A.add(woeT, &m.woeT), A.add(vocR, &m.vocR), A.add(kiteR, &m.kiteR);
+
   A.upload(ctx);
   ctx.perm[0] = pc, ctx.perm[1] = pe, ctx.perm[2] = pv;
   ctx.iperm[0] = ic, ctx.iperm[1] = ie, ctx.iperm[2] = iv;

@@ -231,6 +231,7 @@ __global__ void k_build_stat(DMesh m, double kappa, double *sdv, double *kw, dou
 // ------------------------------------------------------------ state context
 SwState::~SwState() {
   if (graph) cudaGraphExecDestroy(graph);
+  free_adjoint(*this);
   if (arena) cudaFree(arena);
 }
 
@@ -353,11 +354,29 @@ void sw_create(SwState &s) {
   build_stat(s);
 }
 
-}  // namespace mpaso
+// One RK stage of (h, u) only, on explicit buffers (the adjoint's taping
+// recompute).  Tracers are passive in the sw app, so they are left out.
+void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
+                   const double *u_prev, const double *h_prev, double *u_out, double *h_out,
+                   double *u_acc, double *h_acc, double *u_new, double *h_new, cudaStream_t st) {
+  Stage S = make_stage(s, rk, dt);
+  S.u_in = u_in, S.h_in = h_in, S.u_prev = u_prev, S.h_prev = h_prev;
+  S.u_out = u_out, S.h_out = h_out, S.u_acc = u_acc, S.h_acc = h_acc, S.u_new = u_new, S.h_new = h_new;
+  S.fct = 0, S.hmix = 0;
+  launch_stage_T<0>(s, S, st);
+}
 
-struct mpaso_state_s {
-  mpaso::SwState s;
-};
+// Diagnostics (pv, vorticity, ke, divergence) of an explicit (u, h).
+void sw_diag_ptrs(SwState &s, const double *u, const double *h, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  Stage S = make_stage(s, 0, 0.0);
+  S.u_in = u, S.h_in = h;
+  k_sw_diag<<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+}
+
+void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st) { sw_steps(s, dt, nsteps, st); }
+
+}  // namespace mpaso
 
 using namespace mpaso;
 

@@ -71,12 +71,20 @@ struct SwState {
   double graph_dt = 0.0;
   // optional per-launch timing: events recorded after every kernel of a stage
   cudaEvent_t *prof_events = nullptr;
+  // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu
+  struct AdjBuffers *adj = nullptr;
   ~SwState();
 };
 
 // Allocates the state buffers listed as (pointer, doubles) in one arena.
 void alloc_arena(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs);
 void build_stat(SwState &s);
+void free_adjoint(SwState &s);
+void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
+                   const double *u_prev, const double *h_prev, double *u_out, double *h_out,
+                   double *u_acc, double *h_acc, double *u_new, double *h_new, cudaStream_t st);
+void sw_diag_ptrs(SwState &s, const double *u, const double *h, cudaStream_t st);
+void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // FCT / del2 tracer device code (apps/ocean/tasks/solve.cc:99-366).
@@ -213,3 +221,7 @@ __device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S,
 }
 
 }  // namespace mpaso
+
+struct mpaso_state_s {
+  mpaso::SwState s;
+};

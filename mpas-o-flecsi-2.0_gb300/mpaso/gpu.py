@@ -244,6 +244,24 @@ class State:
                                         names, 256))
         return dict(zip(names.value.decode().split(","), list(ms)[:n.value]))
 
+    # ---- differentiation (sw app: h and u) ----
+    def forward(self, dt, nsteps, ckpt_every):
+        """Advances nsteps from the current (h, u), keeping a checkpoint every ckpt_every steps."""
+        check(lib().mpaso_rk4_forward(self._h, ctypes.c_double(dt), int(nsteps), int(ckpt_every)))
+
+    def vjp(self, gh, gu, out=None):
+        """Cotangents of the initial (h, u) from cotangents of the final (h, u) of the last forward."""
+        gh0, gu0 = out if out is not None else (np.empty(self._shape(FIELD_H)), np.empty(self._shape(FIELD_U)))
+        gh = np.ascontiguousarray(gh, np.float64) if isinstance(gh, np.ndarray) else gh
+        gu = np.ascontiguousarray(gu, np.float64) if isinstance(gu, np.ndarray) else gu
+        check(lib().mpaso_rk4_vjp(self._h, _ptr(gh), _ptr(gu), _ptr(gh0), _ptr(gu0)))
+        return gh0, gu0
+
+    def adjoint_device_bytes(self):
+        b = ctypes.c_int64()
+        check(lib().mpaso_adjoint_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
     def launches_per_step(self):
         n = ctypes.c_int32()
         check(lib().mpaso_state_launches_per_step(self._h, ctypes.byref(n)))

@@ -30,11 +30,15 @@ def splitmix64(x):
 def _sphere_field(rng, xyz, degree):
     """Random smooth field on the unit sphere: polynomial of the given degree."""
     x, y, z = xyz
+    px, py, pz = [np.ones_like(x)], [np.ones_like(x)], [np.ones_like(x)]
+    for _ in range(degree):
+        px.append(px[-1] * x), py.append(py[-1] * y), pz.append(pz[-1] * z)
     out = np.zeros_like(x)
     for a in range(degree + 1):
         for b in range(degree + 1 - a):
+            xy = px[a] * py[b]
             for c in range(degree + 1 - a - b):
-                out += rng.standard_normal() * x ** a * y ** b * z ** c
+                out += rng.standard_normal() * (xy * pz[c])
     return out
 
 
