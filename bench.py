@@ -145,6 +145,9 @@ def gpu_arm(args, cfg):
         st.set(f, a)
     dt, K, W = cfg["dt"], args.steps, args.warmup
     ext = torch.cuda.ExternalStream(st.stream())
+    # per-mesh launch autotuning at set-up (untimed; the state is restored after it)
+    launch = st.autotune(dt, 3) if not args.no_autotune else st.launch_config()
+    log(f"launch configuration: {launch}")
     st.step_graph(dt, W)
     st.sync()
 
@@ -253,7 +256,8 @@ def gpu_arm(args, cfg):
                        "tracers": cfg["T"], "dt_s": dt, "fct": cfg["fct"], "del2_tracer": cfg["kappa"],
                        "del2_momentum": cfg["nu"], "parallelism": f"replicas x{world}",
                        "l2": f"device working set {working_set / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2 "
-                             "(no flush)", "timing": "CUDA events on the state stream, graph-replayed steps"},
+                             "(no flush)", "timing": "CUDA events on the state stream, graph-replayed steps",
+                       "launch": dict(launch, autotuned=not args.no_autotune)},
             "roofline": roofline, "fp64": fp64, "step_hbm": step_hbm,
             "kernels_ms_per_launch": {k: round(v, 5) for k, v in prof.items()},
             "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu,
@@ -374,9 +378,10 @@ def ensemble_arm(args):
     from mpaso.ensemble import build
     from mpaso.initial import sw_state
     rng = np.random.default_rng(2024)
-    sides = [32, 48, 64, 96, 128, 192, 256]
+    sides = [int(x) for x in args.ens_sides.split(",")]
+    levels = [int(x) for x in args.ens_levels.split(",")]
     specs = [("hex", int(s), int(s), 10e3, 1e-4) for s in rng.choice(sides, args.ens_planar)]
-    specs += [("icosa", int(l)) for l in rng.choice([5, 6], args.ens_sphere)]
+    specs += [("icosa", int(l)) for l in rng.choice(levels, args.ens_sphere)] if args.ens_sphere else []
     t0 = time.time()
     u, fct, offs, members, mfct = build(specs, nlev=1, return_member_fct=True)
     states = [sw_state(m, 5000 + i, 1, 1) for i, m in enumerate(members)]
@@ -388,6 +393,7 @@ def ensemble_arm(args):
     for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
         st.set(f, np.concatenate([s[k] for s in states]))
     ext = torch.cuda.ExternalStream(st.stream())
+    launch = st.autotune(dt, 3) if not args.no_autotune else st.launch_config()
     st.step_graph(dt, W)
     st.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -396,13 +402,15 @@ def ensemble_arm(args):
     e1.record(ext)
     e1.synchronize()
     t_batch = e0.elapsed_time(e1) * 1e-3
-    # one member at a time: its own context and graph, members advanced in turn
+    # one member at a time: its own context and graph (same launch shapes),
+    # members advanced in turn
     singles = []
     for i, m in enumerate(members):
         d = G.DeviceMesh(m, fct=mfct[i], reorder=False)
         s = G.State(d, nlev=1, ntr=1, **opts)
         for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
             s.set(f, states[i][k])
+        s.set_launch_config(launch["unroll"], launch["threads"])
         s.step_graph(dt, W)
         singles.append((d, s))
     torch.cuda.synchronize()
@@ -416,9 +424,9 @@ def ensemble_arm(args):
     return {"metric": "ensemble members*steps/s (one graph-captured launch sequence vs one at a time)",
             "value": n * K / t_batch, "unit": "member-steps/s", "higher_is_better": True, "n_gpus": 1,
             "steps": K, "warmup": W, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
-            "config": {"workload": f"{args.ens_planar} periodic hex (sides 32..256) + {args.ens_sphere} "
-                                   f"sphere (level 5/6) members, sw + FCT tracer + del2, dt={dt}s",
-                       "cells": int(u.nCells), "edges": int(u.nEdges), "members": n},
+            "config": {"workload": f"{args.ens_planar} periodic hex (sides {args.ens_sides}) + {args.ens_sphere} "
+                                   f"sphere (levels {args.ens_levels}) members, sw + FCT tracer + del2, dt={dt}s",
+                       "cells": int(u.nCells), "edges": int(u.nEdges), "members": n, "launch": launch},
             "cell_updates_per_s": u.nCells * K / t_batch,
             "one_at_a_time": {"value": n * K / t_single, "unit": "member-steps/s",
                               "cell_updates_per_s": u.nCells * K / t_single},
@@ -507,7 +515,10 @@ def main():
     ap.add_argument("--adj-dirs", type=int, default=32)
     ap.add_argument("--ens-planar", type=int, default=192)
     ap.add_argument("--ens-sphere", type=int, default=64)
+    ap.add_argument("--ens-sides", default="32,48,64,96,128,192,256", help="hex member sides to draw from")
+    ap.add_argument("--ens-levels", default="5,6", help="sphere member levels to draw from")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--ref-max-steps", type=int, default=4, help="reference arm: steps timed per process")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm: processes (0 = all cores)")
     args = ap.parse_args()

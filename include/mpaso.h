@@ -219,6 +219,40 @@ int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per
 int mpaso_state_launches_per_step(mpaso_state s, int32_t *n);
 int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
 
+/* Launch configuration of the three kernels of an RK stage, as 6 ints:
+ * config[0..2] = 1 where the kernel's stencil loop is unrolled at compile
+ * time (only meaningful where the mesh's widest stencil is 10: the sphere),
+ * config[3..5] = threads per block (64, 128 or 256).  Results do not depend
+ * on the threads per block; the unrolled and runtime-width variants differ
+ * at most in the last bit.  No counterpart in the reference (its tasks have
+ * no device launch shape).  Setting it drops any captured step graph. */
+int mpaso_state_launch_config(mpaso_state s, int32_t *config);
+int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
+/* Per-mesh autotuner: for each stage kernel in turn, times every variant
+ * (unrolled or not x 64/128/256 threads) over nsteps steps of size dt and
+ * keeps the fastest.  The prognostic state is saved first and restored on
+ * return, so the call leaves (h, u, tracers) unchanged; it allocates one
+ * temporary copy of them.  config (may be NULL) receives the chosen
+ * configuration.  Call it outside stream capture. */
+int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config);
+
+/* Adjoint of the sw RK4 step for (h, u).  No counterpart in the reference,
+ * which has no adjoint: these differentiate what mpaso_rk4_step computes for
+ * app = MPASO_APP_SW (apps/sw/run.cc:10-60) with fct = hmix = 0 semantics
+ * for the tracers (passive) and pin_u = 0.
+ *
+ * mpaso_rk4_forward: advances the state nsteps steps of size dt like
+ * mpaso_rk4_step, keeping a checkpoint of (h, u) every ckpt_every steps.
+ * mpaso_rk4_vjp: given the cotangents gh (nCells x nlev) and gu (nEdges x
+ * nlev) of the state after the forward run, writes dJ/dh0 and dJ/du0 of the
+ * state before it into gh0 / gu0 (reference ordering; host or device
+ * pointers).  Stage states are recomputed segment by segment from the
+ * checkpoints.  Device memory: ceil(N / ckpt_every) + 4 ckpt_every + 2
+ * copies of (h, u) plus about 20 work arrays of one level-field each. */
+int mpaso_rk4_forward(mpaso_state s, double dt, int32_t nsteps, int32_t ckpt_every);
+int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0, double *gu0);
+int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);
+
 /* FP64 ceiling of `device`: DFMA lane-operations per second issued by a
  * compute-only probe kernel (GB300 runs FP64 at a small fraction of FP32). */
 int mpaso_probe_fp64(int device, double *dfma_per_s);

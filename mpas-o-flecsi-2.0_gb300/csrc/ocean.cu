@@ -36,14 +36,14 @@ __global__ void k_oc_prep(DMesh m, DStat st, int L, const double *u, const doubl
   hpi[i] = 1.0 / fma(dt * m.invAreaCell[c], acc, h[i]);
 }
 
-template <int T>
+template <int T, int NA>
 __global__ void __launch_bounds__(TPB) k_oc_edges(DMesh m, DStat st, Stage S, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
   const int2 c = m.coe[e];
-  edge_tracer_fluxes<T>(m, st, S, L, e, k, i, (int64_t)c.x * L + k, (int64_t)c.y * L + k, S.F[i],
-                        S.hE[i]);
+  edge_tracer_fluxes<T, NA>(m, S, L, e, k, i, (int64_t)c.x * L + k, (int64_t)c.y * L + k, S.F[i], S.hE[i],
+                            m.dvEdge, st.cpm1, st.kd);
 }
 
 template <int T>
@@ -100,11 +100,15 @@ template <int T> void ocean_stage_T(SwState &s, const Stage &S, cudaStream_t st)
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
   cudaEvent_t *ev = s.prof_events;
-  k_oc_edges<T><<<blocks_for((int64_t)m.nE * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  const int b0 = s.tune_tpb[0], b1 = s.tune_tpb[1], b2 = s.tune_tpb[2];
+  if (m.maxAdv == 10 && s.tune_unroll[0])
+    k_oc_edges<T, 10><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
+  else
+    k_oc_edges<T, 0><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
-  k_oc_cells<T><<<blocks_for((int64_t)m.nC * L, TPB), TPB, 0, st>>>(m, S, L);
+  k_oc_cells<T><<<blocks_for((int64_t)m.nC * L, b1), b1, 0, st>>>(m, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
-  k_oc_final<T><<<blocks_for((int64_t)m.nC * L, TPB), TPB, 0, st>>>(m, S, L);
+  k_oc_final<T><<<blocks_for((int64_t)m.nC * L, b2), b2, 0, st>>>(m, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
@@ -117,9 +121,8 @@ void ocean_create(SwState &s) {
       {&s.U[0], nE * L}, {&s.H[0], nC * L}, {&s.HE, nE * L}, {&s.HPI, nC * L},
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
       {&s.F, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T}, {&s.DF, nE * L * T},
-      {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T},
-      {(double **)&s.st.sdv, (int64_t)m.maxEoC * nC}, {(double **)&s.st.kw, nE},
-      {(double **)&s.st.sdc, 3 * nV}, {(double **)&s.st.dhs, nE}, {(double **)&s.st.kd, nE}};
+      {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T}};
+  stat_buffers(s, bufs);
   alloc_arena(s, bufs);
   build_stat(s);
 }

@@ -31,7 +31,9 @@ namespace {
 
 constexpr int TPB = 256;
 // ------------------------------------------------------------- K1: edges
-template <int T>
+// NW = 10: edgesOnEdge and advection stencils of exactly 10 slots (hexagon /
+// pentagon meshes), unrolled at compile time; NW = 0: runtime widths.
+template <int T, int NW>
 __global__ void __launch_bounds__(TPB) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
@@ -39,40 +41,42 @@ __global__ void __launch_bounds__(TPB) k_sw_edge_pre(DMesh m, DStat st, Stage S,
   const int2 c = m.coe[e];
   const int2 v = m.voe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-  const double he = 0.5 * (S.h_in[i1] + S.h_in[i2]);
-  const double F = S.u_in[i] * he;
-  const double pve = 0.5 * (S.pv[(int64_t)v.x * L + k] + S.pv[(int64_t)v.y * L + k]);
+  const double hs = S.h_in[i1] + S.h_in[i2];  // 2 h_edge
+  const double F = S.u_in[i] * hs;            // 2 u h_edge
+  const double pv2 = S.pv[(int64_t)v.x * L + k] + S.pv[(int64_t)v.y * L + k];  // 2 pv_edge
   S.F[i] = F;
-  S.G[i] = F * pve;
-  S.pve[i] = pve;
-  if constexpr (T > 0) edge_tracer_fluxes<T>(m, st, S, L, e, k, i, i1, i2, F, he);
+  S.G[i] = F * pv2;
+  S.pve[i] = pv2;
+  if constexpr (T > 0) edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, F, hs, st.dvh, st.cpm2, st.kdh);
 }
 
 // ------------------------------------------------------ K2: edges + cells
-template <int T>
+template <int T, int NW>
 __global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nEL = (int64_t)m.nE * L;
   if (i < nEL) {
     const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
+    // q = sum_j W_j F_j (pv_e + pv_j) / 2 = (Pv_e sum W/8 F2_j + sum W/8 F2_j Pv_j)
     double s1 = 0.0, s2 = 0.0;
-    for (int j = 0; j < m.maxEoE; ++j) {
+    const int ne = NW > 0 ? NW : m.maxEoE;
+#pragma unroll
+    for (int j = 0; j < ne; ++j) {
       const int eo = m.eoe[(int64_t)j * m.nE + e];
-      const double w = m.woe[(int64_t)j * m.nE + e];
+      const double w = st.woe8[(int64_t)j * m.nE + e];
       const int64_t io = (int64_t)eo * L + k;
       s1 = fma(w, S.F[io], s1);
       s2 = fma(w, S.G[io], s2);
     }
-    const double q = 0.5 * fma(S.pve[i], s1, s2);
+    const double q = fma(S.pve[i], s1, s2);
     const int2 c = m.coe[e];
     const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
     const double dh = (S.h_in[i2] - S.h_in[i1]) + st.dhs[e];
-    double tend = q - fma(S.g, dh, S.ke[i2] - S.ke[i1]) * m.invDcEdge[e];
-    if (S.visc) {
+    double tend = fma(-m.invDcEdge[e], fma(S.g, dh, S.ke[i2] - S.ke[i1]), q);
+    if (S.visc) {  // + nu ((div2 - div1) / dc - (vort_b - vort_a) / dv)
       const int2 v = m.voe[e];
-      const double dd = (S.divc[i2] - S.divc[i1]) * m.invDcEdge[e];
-      const double dz = (S.vort[(int64_t)v.y * L + k] - S.vort[(int64_t)v.x * L + k]) * m.invDvEdge[e];
-      tend = fma(S.nu, dd - dz, tend);
+      tend = fma(st.nuDc[e], S.divc[i2] - S.divc[i1], tend);
+      tend = fma(-st.nuDv[e], S.vort[(int64_t)v.y * L + k] - S.vort[(int64_t)v.x * L + k], tend);
     }
     const double up = S.u_prev[i];
     switch (S.stage) {
@@ -93,13 +97,11 @@ __global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int
   if (i >= (int64_t)m.nC * L) return;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c];
-  const double inva = m.invAreaCell[c];
-  double acc = 0.0;
+  double tend_h = 0.0;  // sum edgeSign dv F / area, from F2 with the halved weights
   for (int j = 0; j < n; ++j) {
     const int e = m.eoc[(int64_t)j * m.nC + c];
-    acc = fma(st.sdv[(int64_t)j * m.nC + c], S.F[(int64_t)e * L + k], acc);
+    tend_h = fma(st.sdvi[(int64_t)j * m.nC + c], S.F[(int64_t)e * L + k], tend_h);
   }
-  const double tend_h = acc * inva;
   const double hp = S.h_prev[i];
   switch (S.stage) {
     case 0:
@@ -210,20 +212,37 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
 }
 
 // Derived statics of a state.
-__global__ void k_build_stat(DMesh m, double kappa, double *sdv, double *kw, double *sdc,
-                             double *dhs, double *kd) {
+struct StatOut {
+  double *sdv, *sdvi, *kw, *sdc, *dhs, *kd, *kdh, *dvh, *woe8;
+  double2 *cpm2, *cpm1;
+  double *nuDc, *nuDv;
+};
+
+__global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < (int64_t)m.maxEoC * m.nC) {
     const int c = (int)(i % m.nC), j = (int)(i / m.nC);
-    sdv[i] = j < m.nEoC[c] ? m.eocSign[i] * m.dvEdge[m.eoc[i]] : 0.0;
+    const double s = j < m.nEoC[c] ? m.eocSign[i] * m.dvEdge[m.eoc[i]] : 0.0;
+    o.sdv[i] = s;
+    o.sdvi[i] = 0.5 * s * m.invAreaCell[c];
   }
   if (i < m.nE) {
-    kw[i] = 0.25 * m.dcEdge[i] * m.dvEdge[i];
+    o.kw[i] = 0.25 * m.dcEdge[i] * m.dvEdge[i];
     const int2 c = m.coe[i];
-    dhs[i] = m.bottomDepth[c.y] - m.bottomDepth[c.x];
-    kd[i] = m.meshScalingDel2[i] * kappa * m.dvEdge[i] * m.invDcEdge[i];
+    o.dhs[i] = m.bottomDepth[c.y] - m.bottomDepth[c.x];
+    const double kd = m.meshScalingDel2[i] * kappa * m.dvEdge[i] * m.invDcEdge[i];
+    o.kd[i] = kd;
+    o.kdh[i] = 0.5 * kd;
+    o.dvh[i] = 0.5 * m.dvEdge[i];
+    o.nuDc[i] = nu * m.invDcEdge[i];
+    o.nuDv[i] = nu * m.invDvEdge[i];
   }
-  if (i < (int64_t)kVertexDegree * m.nV) sdc[i] = m.eovSign[i] * m.dcEdge[m.eov[i]];
+  if (i < (int64_t)m.maxEoE * m.nE) o.woe8[i] = 0.125 * m.woe[i];
+  if (i < (int64_t)m.maxAdv * m.nE) {
+    o.cpm1[i] = make_double2(m.advCp[i], m.advCm[i]);
+    o.cpm2[i] = make_double2(0.5 * m.advCp[i], 0.5 * m.advCm[i]);
+  }
+  if (i < (int64_t)kVertexDegree * m.nV) o.sdc[i] = m.eovSign[i] * m.dcEdge[m.eov[i]];
 }
 
 }  // namespace
@@ -254,10 +273,27 @@ void alloc_arena(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs) {
 void build_stat(SwState &s) {
   const DMesh &m = s.mesh->ctx.d;
   const int64_t nmax = std::max<int64_t>(std::max<int64_t>(m.nE, 3LL * m.nV), (int64_t)m.maxEoC * m.nC);
-  k_build_stat<<<blocks_for(nmax, TPB), TPB, 0, s.stream>>>(
-      m, s.p.kappa, (double *)s.st.sdv, (double *)s.st.kw, (double *)s.st.sdc, (double *)s.st.dhs,
-      (double *)s.st.kd);
+  const int64_t nmax2 = std::max<int64_t>(nmax, std::max<int64_t>((int64_t)m.maxEoE * m.nE,
+                                                                  (int64_t)m.maxAdv * m.nE));
+  StatOut o{(double *)s.st.sdv, (double *)s.st.sdvi, (double *)s.st.kw, (double *)s.st.sdc,
+            (double *)s.st.dhs, (double *)s.st.kd, (double *)s.st.kdh, (double *)s.st.dvh,
+            (double *)s.st.woe8, (double2 *)s.st.cpm2, (double2 *)s.st.cpm1, (double *)s.st.nuDc,
+            (double *)s.st.nuDv};
+  k_build_stat<<<blocks_for(nmax2, TPB), TPB, 0, s.stream>>>(m, s.p.kappa, s.p.nu, o);
   MPASO_CUDA(cudaGetLastError());
+}
+
+// The derived statics of a state, as (pointer, doubles) arena entries.
+void stat_buffers(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t nC = m.nC, nE = m.nE, nV = m.nV;
+  DStat &t = s.st;
+  auto P = [](const double *&p) { return (double **)&p; };
+  bufs.insert(bufs.end(), {{P(t.sdv), (int64_t)m.maxEoC * nC}, {P(t.sdvi), (int64_t)m.maxEoC * nC},
+                           {P(t.kw), nE}, {P(t.sdc), 3 * nV}, {P(t.dhs), nE}, {P(t.kd), nE},
+                           {P(t.kdh), nE}, {P(t.dvh), nE}, {P(t.woe8), (int64_t)m.maxEoE * nE},
+                           {(double **)&t.cpm2, 2LL * m.maxAdv * nE},
+                           {(double **)&t.cpm1, 2LL * m.maxAdv * nE}, {P(t.nuDc), nE}, {P(t.nuDv), nE}});
 }
 
 namespace {
@@ -289,11 +325,19 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
   cudaEvent_t *ev = s.prof_events;
-  k_sw_edge_pre<T><<<blocks_for((int64_t)m.nE * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0);
+  const int b0 = s.tune_tpb[0], b1 = s.tune_tpb[1], b2 = s.tune_tpb[2];
+  if (w10 && s.tune_unroll[0])
+    k_sw_edge_pre<T, 10><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
+  else
+    k_sw_edge_pre<T, 0><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
-  k_sw_tend<T><<<blocks_for(((int64_t)m.nE + m.nC) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  if (w10 && s.tune_unroll[1])
+    k_sw_tend<T, 10><<<blocks_for(((int64_t)m.nE + m.nC) * L, b1), b1, 0, st>>>(m, s.st, S, L);
+  else
+    k_sw_tend<T, 0><<<blocks_for(((int64_t)m.nE + m.nC) * L, b1), b1, 0, st>>>(m, s.st, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
-  k_sw_final<T><<<blocks_for(((int64_t)m.nC + m.nV) * L, TPB), TPB, 0, st>>>(m, s.st, S, L);
+  k_sw_final<T><<<blocks_for(((int64_t)m.nC + m.nV) * L, b2), b2, 0, st>>>(m, s.st, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
@@ -347,9 +391,8 @@ void sw_create(SwState &s) {
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
       {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.ke, nC * L}, {&s.divc, nC * L},
       {&s.F, nE * L}, {&s.G, nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
-      {&s.DF, nE * L * T}, {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T},
-      {(double **)&s.st.sdv, (int64_t)m.maxEoC * nC}, {(double **)&s.st.kw, nE},
-      {(double **)&s.st.sdc, 3 * nV}, {(double **)&s.st.dhs, nE}, {(double **)&s.st.kd, nE}};
+      {&s.DF, nE * L * T}, {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T}};
+  stat_buffers(s, bufs);
   alloc_arena(s, bufs);
   build_stat(s);
 }
@@ -402,6 +445,62 @@ void run_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
   else
     sw_steps(s, dt, nsteps, st);
 }
+
+// Device time (ms per launch) of the three stage kernels over nsteps RK4
+// steps, from events recorded between the launches; advances the state.
+void time_stage_kernels(SwState &S, double dt, int nsteps, double ms[3]) {
+  const bool oc = S.p.app == MPASO_APP_OCEAN;
+  constexpr int nk = 3;
+  if (oc)
+    ocean_prepare(S, dt, S.stream);
+  else
+    ensure_diag(S, S.stream);
+  cudaEvent_t ev[nk + 1] = {};
+  double acc[nk] = {0, 0, 0};
+  try {
+    for (auto &e : ev) MPASO_CUDA(cudaEventCreate(&e));
+    S.prof_events = ev + 1;
+    for (int n = 0; n < nsteps; ++n)
+      for (int rk = 0; rk < 4; ++rk) {
+        MPASO_CUDA(cudaEventRecord(ev[0], S.stream));
+        if (oc)
+          ocean_one_stage(S, rk, dt, S.stream);
+        else
+          launch_stage(S, make_stage(S, rk, dt), S.stream);
+        MPASO_CUDA(cudaEventSynchronize(ev[nk]));
+        for (int k = 0; k < nk; ++k) {
+          float t = 0.f;
+          MPASO_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+          acc[k] += t;
+        }
+      }
+  } catch (...) {
+    S.prof_events = nullptr;
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+    throw;
+  }
+  S.prof_events = nullptr;
+  for (auto &e : ev) MPASO_CUDA(cudaEventDestroy(e));
+  for (int k = 0; k < nk; ++k) ms[k] = acc[k] / (4.0 * nsteps);
+}
+
+// A captured step graph bakes in the launch shapes; drop it when they change.
+void drop_graph(SwState &S) {
+  if (S.graph) {
+    MPASO_CUDA(cudaGraphExecDestroy(S.graph));
+    S.graph = nullptr;
+  }
+}
+
+// Whether kernel k of the stage has a compile-time-unrolled variant on this mesh.
+bool has_unrolled(const SwState &S, int k) {
+  const DMesh &m = S.mesh->ctx.d;
+  if (S.p.app == MPASO_APP_OCEAN) return k == 0 && m.maxAdv == 10;
+  return k < 2 && m.maxEoE == 10 && (m.maxAdv == 10 || !S.p.fct || S.T == 0);
+}
+
+constexpr int kTpbChoices[3] = {64, 128, 256};
 
 }  // namespace
 
@@ -562,39 +661,8 @@ int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     const bool oc = S.p.app == MPASO_APP_OCEAN;
     const char *kinds = oc ? "oc_edges,oc_cells,oc_final" : "sw_edge_pre,sw_tend,sw_final";
-    const int nk = 3;
-    if (oc)
-      ocean_prepare(S, dt, S.stream);
-    else
-      ensure_diag(S, S.stream);
-    std::vector<cudaEvent_t> ev(nk + 1);
-    for (auto &e : ev) MPASO_CUDA(cudaEventCreate(&e));
-    double acc[8] = {0};
-    S.prof_events = ev.data() + 1;
-    try {
-      for (int n = 0; n < nsteps; ++n)
-        for (int rk = 0; rk < 4; ++rk) {
-          MPASO_CUDA(cudaEventRecord(ev[0], S.stream));
-          if (oc)
-            ocean_one_stage(S, rk, dt, S.stream);
-          else
-            launch_stage(S, make_stage(S, rk, dt), S.stream);
-          MPASO_CUDA(cudaEventSynchronize(ev[nk]));
-          for (int k = 0; k < nk; ++k) {
-            float ms = 0.f;
-            MPASO_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
-            acc[k] += ms;
-          }
-        }
-    } catch (...) {
-      S.prof_events = nullptr;
-      for (auto &e : ev) cudaEventDestroy(e);
-      throw;
-    }
-    S.prof_events = nullptr;
-    for (auto &e : ev) MPASO_CUDA(cudaEventDestroy(e));
-    for (int k = 0; k < nk; ++k) ms_per_launch[k] = acc[k] / (4.0 * nsteps);
-    *nkinds = nk;
+    time_stage_kernels(S, dt, nsteps, ms_per_launch);
+    *nkinds = 3;
     if (names && names_len > 0) {
       std::strncpy(names, kinds, (size_t)names_len - 1);
       names[names_len - 1] = 0;
@@ -627,6 +695,85 @@ int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes) {
   return guarded("mpaso_state_device_bytes", [&] {
     require(s && bytes, MPASO_ERR_ARG, "null argument");
     *bytes = (int64_t)s->s.arena_bytes;
+  });
+}
+
+int mpaso_state_launch_config(mpaso_state s, int32_t *config) {
+  return guarded("mpaso_state_launch_config", [&] {
+    require(s && config, MPASO_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k) config[k] = s->s.tune_unroll[k], config[3 + k] = s->s.tune_tpb[k];
+  });
+}
+
+int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
+  return guarded("mpaso_state_set_launch_config", [&] {
+    require(s && config, MPASO_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k) {
+      require(config[k] == 0 || config[k] == 1, MPASO_ERR_ARG, "unroll flag must be 0 or 1");
+      const int b = config[3 + k];
+      require(b == 64 || b == 128 || b == 256, MPASO_ERR_ARG, "threads per block must be 64, 128 or 256");
+    }
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+    drop_graph(S);
+    for (int k = 0; k < 3; ++k) S.tune_unroll[k] = config[k], S.tune_tpb[k] = config[3 + k];
+  });
+}
+
+int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config) {
+  return guarded("mpaso_state_autotune", [&] {
+    require(s && nsteps > 0 && dt > 0.0, MPASO_ERR_ARG, "bad argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+    const DMesh &m = S.mesh->ctx.d;
+    // Every candidate starts from the same prognostic state, which is put
+    // back at the end: (h, u, tracers) are the only fields a step reads that
+    // it also overwrites.
+    const size_t nh = (size_t)m.nC * S.L, nu = (size_t)m.nE * S.L, nt = (size_t)m.nC * S.L * S.T;
+    double *keep = nullptr;
+    MPASO_CUDA(cudaMalloc((void **)&keep, (nh + nu + nt) * sizeof(double)));
+    auto save_restore = [&](bool save) {
+      const std::pair<double *, size_t> f[3] = {{S.H[0], nh}, {S.U[0], nu}, {S.TR0, nt}};
+      size_t off = 0;
+      for (const auto &x : f) {
+        if (x.second) {
+          double *a = save ? keep + off : x.first;
+          const double *b = save ? x.first : keep + off;
+          MPASO_CUDA(cudaMemcpyAsync(a, b, x.second * sizeof(double), cudaMemcpyDeviceToDevice, S.stream));
+        }
+        off += x.second;
+      }
+      S.diag_valid = false;
+    };
+    try {
+      drop_graph(S);
+      save_restore(true);
+      double ms[3];
+      time_stage_kernels(S, dt, 1, ms);  // warm-up
+      for (int k = 0; k < 3; ++k) {
+        double best = 1e300;
+        int best_u = S.tune_unroll[k], best_b = S.tune_tpb[k];
+        for (int u = has_unrolled(S, k) ? 1 : 0; u >= 0; --u)
+          for (int b : kTpbChoices) {
+            S.tune_unroll[k] = u, S.tune_tpb[k] = b;
+            save_restore(false);
+            time_stage_kernels(S, dt, nsteps, ms);
+            if (ms[k] < best) best = ms[k], best_u = u, best_b = b;
+          }
+        S.tune_unroll[k] = best_u, S.tune_tpb[k] = best_b;
+      }
+      save_restore(false);
+      MPASO_CUDA(cudaStreamSynchronize(S.stream));
+    } catch (...) {
+      cudaStreamSynchronize(S.stream);
+      cudaFree(keep);
+      throw;
+    }
+    MPASO_CUDA(cudaFree(keep));
+    if (config)
+      for (int k = 0; k < 3; ++k) config[k] = S.tune_unroll[k], config[3 + k] = S.tune_tpb[k];
   });
 }
 

@@ -26,12 +26,24 @@ __device__ __forceinline__ double rcp_nr(double b) {
 __device__ __forceinline__ long long sign_mask(double s) { return dbits(s) & kSignBit; }
 
 // Per-state derived statics (device arrays), built once at state creation.
+// The sw kernels carry the doubled thickness flux F2 = u (h1 + h2) = 2 F and
+// the doubled edge PV Pv = pv_a + pv_b = 2 pv_e; the power-of-two factors are
+// folded into the scaled copies below, which changes no rounding.
 struct DStat {
-  const double *sdv;  // [maxEoC][nC] edgeSignOnCell * dvEdge (0 in pad slots)
-  const double *kw;   // [nE] 0.25 * dcEdge * dvEdge
-  const double *sdc;  // [3][nV] circulation sign * dcEdge
-  const double *dhs;  // [nE] h_s(c2) - h_s(c1)
-  const double *kd;   // [nE] meshScalingDel2 * kappa * dvEdge / dcEdge
+  const double *sdv;   // [maxEoC][nC] edgeSignOnCell * dvEdge (0 in pad slots)
+  const double *sdvi;  // [maxEoC][nC] 0.5 * edgeSignOnCell * dvEdge / areaCell (tend_h from F2)
+  const double *kw;    // [nE] 0.25 * dcEdge * dvEdge
+  const double *sdc;   // [3][nV] circulation sign * dcEdge
+  const double *dhs;   // [nE] h_s(c2) - h_s(c1)
+  const double *kd;    // [nE] meshScalingDel2 * kappa * dvEdge / dcEdge
+  const double *kdh;   // [nE] kd / 2 (del2 flux from h1 + h2)
+  const double *dvh;   // [nE] dvEdge / 2 (fluxes from F2)
+  const double *woe8;  // [maxEoE][nE] weightsOnEdge / 8 (PV flux from F2, Pv)
+  // [maxAdv][nE] pairs {advCoef + 0.25 advCoef_3rd, advCoef - 0.25 advCoef_3rd}, halved
+  // (cpm2, sw kernels) or not (cpm1, ocean kernels); one 16-byte load per slot, the
+  // flux sign picks the member.
+  const double2 *cpm2, *cpm1;
+  const double *nuDc, *nuDv;  // [nE] nu / dcEdge, nu / dvEdge
 };
 
 // One RK stage's pointers and weights.
@@ -73,12 +85,17 @@ struct SwState {
   cudaEvent_t *prof_events = nullptr;
   // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu
   struct AdjBuffers *adj = nullptr;
+  // launch configuration of the three stage kernels (autotuned): stencil
+  // unrolled at compile time (1) or runtime width (0), threads per block
+  int tune_unroll[3] = {1, 1, 1};
+  int tune_tpb[3] = {256, 256, 256};
   ~SwState();
 };
 
 // Allocates the state buffers listed as (pointer, doubles) in one arena.
 void alloc_arena(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs);
 void build_stat(SwState &s);
+void stat_buffers(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs);
 void free_adjoint(SwState &s);
 void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
                    const double *u_prev, const double *h_prev, double *u_out, double *h_out,
@@ -91,25 +108,32 @@ void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
 
 // Edge fluxes for tracers of the stage input: low-order flux LO, anti-
 // diffusive flux A = HO - LO, del2 flux DF = h_e (tr2 - tr1) kappa ...
-template <int T>
-__device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const DStat &st, const Stage &S,
-                                                   int L, int e, int k, int64_t i, int64_t i1,
-                                                   int64_t i2, double F, double he) {
+// The thickness flux arrives as F = s * u h_e (s = 1 or 2) and the edge
+// thickness as hx = s * h_e; dv, cp, cm, kd are the matching 1/s copies.
+// NA > 0: compile-time advection-stencil width (the mesh's maxAdv); 0 = runtime.
+template <int T, int NA>
+__device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &S, int L, int e, int k,
+                                                   int64_t i, int64_t i1, int64_t i2, double F,
+                                                   double hx, const double *dv, const double2 *cpm,
+                                                   const double *kd) {
   double t1[T], t2[T];
 #pragma unroll
   for (int t = 0; t < T; ++t) t1[t] = S.tr_in[i1 * T + t], t2[t] = S.tr_in[i2 * T + t];
-  const double dvF = m.dvEdge[e] * F;
+  const double dvF = dv[e] * F;
   if (S.fct) {
     // low order: dv (max(0,F) tr1 + min(0,F) tr2) == dv F tr_upwind (ocean solve.cc:110-113)
     const bool up1 = dgt0(F);
     // high order: F mask sum_a tr_a (advCoef_a + 0.25 advCoef_3rd_a sign(F)) (solve.cc:137-165)
-    const double *coef = dlt0(F) ? m.advCm : m.advCp;
+    const bool neg = dlt0(F);
     double s[T];
 #pragma unroll
     for (int t = 0; t < T; ++t) s[t] = 0.0;
-    for (int a = 0; a < m.maxAdv; ++a) {
+    const int na = NA > 0 ? NA : m.maxAdv;
+#pragma unroll
+    for (int a = 0; a < na; ++a) {
       const int cell = m.advCells[(int64_t)a * m.nE + e];
-      const double cf = coef[(int64_t)a * m.nE + e];
+      const double2 c2 = cpm[(int64_t)a * m.nE + e];
+      const double cf = neg ? c2.y : c2.x;
       const double *tr = S.tr_in + ((int64_t)cell * L + k) * T;
 #pragma unroll
       for (int t = 0; t < T; ++t) s[t] = fma(cf, tr[t], s[t]);
@@ -130,7 +154,7 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const DStat &
     for (int t = 0; t < T; ++t) S.LO[i * T + t] = (0.5 * dvF) * (t1[t] + t2[t]);
   }
   if (S.hmix) {
-    const double hk = he * st.kd[e];
+    const double hk = hx * kd[e];
 #pragma unroll
     for (int t = 0; t < T; ++t) S.DF[i * T + t] = hk * (t2[t] - t1[t]);
   }
@@ -150,11 +174,12 @@ __device__ __forceinline__ void cell_limiter(const DMesh &m, const Stage &S, int
         const int e = m.eoc[(int64_t)j * m.nC + c];
         tl += dflip(S.LO[((int64_t)e * L + k) * T + t], sign_mask(m.eocSign[(int64_t)j * m.nC + c]));
       }
-      S.tLO[i * T + t] = tl * inva;
+      S.tLO[i * T + t] = tl;  // area-weighted; cell_tracer_tend divides by the area
     }
     return;
   }
-  const double dth = S.dt * hpi;
+  const double dtia = S.dt * inva;  // dt / area
+  const double dthi = dtia * hpi;   // dt / (area hProv)
   const double eps = 1.e-10;
 #pragma unroll
   for (int t = 0; t < T; ++t) {
@@ -173,13 +198,11 @@ __device__ __forceinline__ void cell_limiter(const DMesh &m, const Stage &S, int
       fi += dpos(ax);
       fo += dneg(ax);
     }
-    tl *= inva;
-    fi *= inva;
-    fo *= inva;
-    const double up = fma(S.dt, tl, trc * hin) * hpi;
-    const double mxn = fma(dth, fi, up), mnn = fma(dth, fo, up);
-    const double np = mx - up, dp = (mxn - up) + eps;
-    const double nm = up - mn, dm = (up - mnn) + eps;
+    // trUp = (tr h + dt tend) / hProv; trMaxNew - trUp = dt flxIn / hProv, with
+    // tend, flxIn, flxOut the area-weighted sums tl, fi, fo divided by the area
+    const double up = fma(dtia, tl, trc * hin) * hpi;
+    const double np = mx - up, dp = fma(dthi, fi, eps);
+    const double nm = up - mn, dm = fma(-dthi, fo, eps);
     // clamp01(n / d): 0 when n <= 0, 1 when n >= d, the quotient otherwise
     double rp = dgt0(np) ? 1.0 : 0.0, rm = dgt0(nm) ? 1.0 : 0.0;
     if (dgt0(np) && dkey(np) < dkey(dp)) rp = dclamp01(np * rcp_nr(dp));
@@ -199,7 +222,7 @@ __device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S,
   const double inva = m.invAreaCell[c];
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    double acc = 0.0;
+    double acc = S.tLO[i * T + t];  // area-weighted upwind part
     for (int j = 0; j < n; ++j) {
       const int e = m.eoc[(int64_t)j * m.nC + c];
       const long long sm = sign_mask(m.eocSign[(int64_t)j * m.nC + c]);
@@ -216,7 +239,7 @@ __device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S,
       if (S.hmix) x -= S.DF[ie];
       acc += dflip(x, sm);
     }
-    tend[t] = fma(inva, acc, S.tLO[i * T + t]);
+    tend[t] = acc * inva;
   }
 }
 

@@ -244,6 +244,28 @@ class State:
                                         names, 256))
         return dict(zip(names.value.decode().split(","), list(ms)[:n.value]))
 
+    # ---- launch configuration of the three stage kernels ----
+    @staticmethod
+    def _cfg_dict(c):
+        return {"unroll": [int(x) for x in c[:3]], "threads": [int(x) for x in c[3:]]}
+
+    def launch_config(self):
+        """{'unroll': [3 flags], 'threads': [3 block sizes]} of the stage kernels."""
+        c = (ctypes.c_int32 * 6)()
+        check(lib().mpaso_state_launch_config(self._h, c))
+        return self._cfg_dict(c)
+
+    def set_launch_config(self, unroll, threads):
+        c = (ctypes.c_int32 * 6)(*[int(x) for x in list(unroll) + list(threads)])
+        check(lib().mpaso_state_set_launch_config(self._h, c))
+
+    def autotune(self, dt, nsteps=3):
+        """Times every launch variant of each stage kernel on this mesh and keeps
+        the fastest; (h, u, tracers) are restored afterwards.  Returns the choice."""
+        c = (ctypes.c_int32 * 6)()
+        check(lib().mpaso_state_autotune(self._h, ctypes.c_double(dt), int(nsteps), c))
+        return self._cfg_dict(c)
+
     # ---- differentiation (sw app: h and u) ----
     def forward(self, dt, nsteps, ckpt_every):
         """Advances nsteps from the current (h, u), keeping a checkpoint every ckpt_every steps."""

@@ -41,36 +41,38 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
     slot_c = Nc * nC  # ragged cell slots
     # ---- K1 edge pre-pass
     b1 = 8 * nE * 2 + 8 * cl + 8 * el + 8 * vl + 24 * el
-    f1 = 6 * el
+    f1 = 4 * el  # h1 + h2, u hs, pv_a + pv_b, F Pv
     if T:
         b1 += 8 * cl * T + 8 * nE
         f1 += el
         if fct:
-            b1 += 12 * Na * nE + 4 * el + 16 * el * T
+            b1 += 20 * Na * nE + 4 * el + 16 * el * T  # advCells + {cp, cm} pairs, hoMask, LO, A
             f1 += el * T * (Na + 3)
         else:
             b1 += 8 * el * T
-            f1 += 2 * el * T
+            f1 += el * (1 + 2 * T)
         if hmix:
             b1 += 8 * nE + 8 * el * T
             f1 += el * (1 + 2 * T)
     # ---- K2 edges + cells
     b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * nE + 8 * cl + 8 * nE
     b2 += 8 * el + 16 * el + 8 * el * 0.75
-    f2 = el * (2 * Ne + 8 + 1.75)
+    f2 = el * (2 * Ne + 6 + 1.75)
     if visc:
-        b2 += 8 * cl + 8 * vl + 16 * nE
-        f2 += 6 * el
+        b2 += 8 * cl + 8 * vl + 24 * nE
+        f2 += 4 * el
     b2 += 4 * nC + 12 * slot_c + 8 * nC + 8 * cl + 16 * cl + 8 * cl * 0.75
-    f2 += cl * (Nc + 1 + 1.75)
+    f2 += cl * (Nc + 1.75)
     if T:
         b2 += 8 * slot_c
         if fct:
             b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
-            f2 += cl * (7 + T * (3 * Nc + 26))
+            # 1/hProv (6), dt/area, dt/(area hProv); per tracer 3 sums per edge, trUp (3),
+            # numerators / denominators (4), two guarded rcp_nr quotients (12)
+            f2 += cl * (8 + T * (3 * Nc + 19))
         else:
             b2 += 8 * el * T + 8 * cl * T
-            f2 += cl * T * (Nc + 1)
+            f2 += cl * T * Nc
     # ---- K3 cells + vertices
     b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl  # diag: kw, u_next, invArea, ke
     f3 = cl * (2 * Nc + 1)
@@ -83,7 +85,7 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b3 += 8 * el * T + 16 * cl * T
         if hmix:
             b3 += 8 * el * T
-        f3 += cl * (5 + T * (3 * Nc + 4))
+        f3 += cl * (5 + T * (Nc * (1 + int(fct) + int(hmix)) + 4.75))
     b3 += 8 * nV * (3 + 1.5 + 3 + 1.5 + 3) + 8 * vl + 16 * vl
     f3 += vl * 14
     return {"sw_edge_pre": (b1, f1), "sw_tend": (b2, f2), "sw_final": (b3, f3)}
@@ -98,17 +100,17 @@ def ocean_kernels(d: Dims, fct=True, hmix=True):
     b1 = 8 * nE + 8 * el + 8 * cl * T + 8 * nE + 8 * el  # coe, F, tr_in, dv, hE
     f1 = el
     if fct:
-        b1 += 12 * Na * nE + 4 * el + 16 * el * T
+        b1 += 20 * Na * nE + 4 * el + 16 * el * T
         f1 += el * T * (Na + 3)
     if hmix:
         b1 += 8 * nE + 8 * el * T
         f1 += el * (1 + 2 * T)
     b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
     b2 += 16 * el * T + 24 * cl * T
-    f2 = cl * (1 + T * (3 * Nc + 26))
+    f2 = cl * (2 + T * (3 * Nc + 19))
     b3 = 4 * nC + 12 * slot_c + 8 * nC + 8 * nE + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
     b3 += 8 * el * T * (int(fct) + int(hmix))
-    f3 = cl * T * (3 * Nc + 3)
+    f3 = cl * T * (Nc * (1 + int(fct) + int(hmix)) + 2.75)
     return {"oc_edges": (b1, f1), "oc_cells": (b2, f2), "oc_final": (b3, f3)}
 
 

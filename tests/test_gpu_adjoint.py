@@ -81,3 +81,28 @@ def test_autograd_function_contract():
     gh, gu = st.vjp((hN - target).detach().cpu().numpy(), np.zeros_like(u))
     assert np.allclose(h0.grad.cpu().numpy(), gh, rtol=0, atol=1e-12 * np.abs(gh).max())
     assert np.allclose(u0.grad.cpu().numpy(), gu, rtol=0, atol=1e-12 * np.abs(gu).max())
+
+
+@pytest.mark.parametrize("nu", [0.0, 2e5])
+def test_adjoint_dot_product_against_complex_step(nu):
+    """<w, J v> from the complex-step tangent of the CPU restatement of the
+    reference step equals <J^T w, v> from the CUDA adjoint (relative 1e-10:
+    both are exact derivatives, of functions that agree to rounding)."""
+    import mpaso.gpu as G
+    from sw_complex import SwComplex
+    mesh, dm, st, h, u = make(level=3, L=2, nu=nu)
+    rng = np.random.default_rng(7)
+    wh, wu = rng.standard_normal(h.shape), rng.standard_normal(u.shape) * 100
+    dt, n = 300.0, 6
+    st.set(G.FIELD_H, h)
+    st.set(G.FIELD_U, u)
+    st.forward(dt, n, 2)
+    gh, gu = st.vjp(wh, wu)
+    C = SwComplex(mesh, 2, nu=nu)
+    for _ in range(3):
+        vh, vu = rng.standard_normal(h.shape), rng.standard_normal(u.shape) * 1e-3
+        jh, ju = C.jvp(h, u, vh, vu, dt, n)
+        lhs = float((wh.ravel() * jh.ravel()).sum() + (wu.ravel() * ju.ravel()).sum())
+        rhs = float((gh.ravel() * vh.ravel()).sum() + (gu.ravel() * vu.ravel()).sum())
+        scale = np.abs(wh.ravel() * jh.ravel()).sum() + np.abs(wu.ravel() * ju.ravel()).sum()
+        assert abs(lhs - rhs) <= 1e-10 * scale, (lhs, rhs)

@@ -1,0 +1,91 @@
+"""Launch-configuration variants and the per-mesh autotuner (GPU).
+
+Every launch variant of the stage kernels (stencil unrolled at compile time or
+not; 64/128/256 threads per block) must reproduce the reference goldens at the
+one-step parity bar of the fused path (relative max-norm 1e-12).  Block size
+does not change any thread's arithmetic, so two configurations differing only
+in threads per block agree bit for bit.  The autotuner restores the state it
+timed on, bit for bit."""
+import numpy as np
+import pytest
+
+from helpers import Golden, golden_names, rel_max
+from test_gpu_rk4 import make_state
+
+pytestmark = pytest.mark.gpu
+TOL1 = 1e-12
+
+CONFIGS = [([1, 1, 1], [256, 256, 256]), ([0, 0, 0], [256, 256, 256]), ([1, 1, 1], [64, 128, 64]),
+           ([0, 1, 0], [128, 64, 256])]
+
+
+def _fields(st, app):
+    import mpaso.gpu as G
+    out = [st.get(G.FIELD_TRACERS)]
+    if app == "sw":
+        out += [st.get(G.FIELD_H), st.get(G.FIELD_U)]
+    return out
+
+
+@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("cfg", range(len(CONFIGS)))
+def test_every_launch_variant_matches_goldens(name, cfg):
+    g = Golden(name)
+    dm, st = make_state(g)
+    st.set_launch_config(*CONFIGS[cfg])
+    assert st.launch_config() == {"unroll": CONFIGS[cfg][0], "threads": CONFIGS[cfg][1]}
+    st.step_graph(g.dt, 1)
+    got = _fields(st, g.app)
+    want = [g["tr_1"]] + ([g["h_1"], g["u_1"]] if g.app == "sw" else [])
+    for a, b in zip(got, want):
+        assert rel_max(a, b) < TOL1
+    st.close()
+    dm.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_block_size_is_bitwise_neutral(name):
+    g = Golden(name)
+    res = []
+    for threads in ([256, 256, 256], [64, 128, 64]):
+        dm, st = make_state(g)
+        st.set_launch_config([1, 1, 1], threads)
+        st.step(g.dt, 3)
+        res.append(_fields(st, g.app))
+        st.close()
+        dm.close()
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["sw_fct_icosa3_L1T1", "ocean_icosa3_L3T2"])
+def test_autotune_restores_state_and_keeps_parity(name):
+    g = Golden(name)
+    dm, st = make_state(g)
+    before = _fields(st, g.app)
+    st.step_graph(g.dt, 0)  # captures a step graph with the default launch shapes
+    cfg = st.autotune(g.dt, 2)
+    assert all(b in (64, 128, 256) for b in cfg["threads"]) and all(u in (0, 1) for u in cfg["unroll"])
+    assert st.launch_config() == cfg
+    for a, b in zip(_fields(st, g.app), before):
+        assert np.array_equal(a, b)
+    st.step_graph(g.dt, 1)
+    want = [g["tr_1"]] + ([g["h_1"], g["u_1"]] if g.app == "sw" else [])
+    for a, b in zip(_fields(st, g.app), want):
+        assert rel_max(a, b) < TOL1
+    st.close()
+    dm.close()
+
+
+def test_bad_launch_config_is_rejected():
+    import mpaso
+    g = Golden("sw_hex16_L1T1")
+    dm, st = make_state(g)
+    with pytest.raises(mpaso.MpasoError) as e:
+        st.set_launch_config([1, 1, 1], [256, 512, 256])
+    assert e.value.code == 1
+    with pytest.raises(mpaso.MpasoError):
+        st.set_launch_config([2, 1, 1], [256, 256, 256])
+    assert st.launch_config()["threads"] == [256, 256, 256]
+    st.close()
+    dm.close()

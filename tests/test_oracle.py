@@ -63,3 +63,33 @@ def test_oracle_detects_planted_error():
     h, u, tr = S.sw_run(g.mesh, S.static(g.mesh, fct), S.config(g.L, g.T, **g.opts), g.dt, 1,
                         g["h0"], g["u0"], g["tr0"])
     assert not np.array_equal(tr, g["tr_1"])
+
+
+@pytest.mark.parametrize("kind", ["icosa3", "hex16"])
+@pytest.mark.parametrize("nu", [0.0, 2e5])
+def test_complex_step_restatement(kind, nu):
+    """The complex-step restatement of the sw (h, u) step reproduces the oracle's
+    real step to rounding, and its tangent agrees with central differences of the
+    oracle to the differences' truncation error."""
+    import mpaso
+    from mpaso.initial import sw_state
+    from sw_complex import SwComplex
+    mesh = mpaso.Mesh.icosa(3) if kind == "icosa3" else mpaso.Mesh.hex(16, 16, 10e3)
+    dt, L, n = (300.0 if kind == "icosa3" else 30.0), 2, 3
+    S = Oracle("restatement")
+    h, u, tr = sw_state(mesh, 3, L, 1)
+    run = lambda hh, uu: S.sw_run(mesh, S.static(mesh), S.config(L, 1, nu=nu), dt, n, hh, uu, tr)  # noqa: E731
+    hr, ur, _ = run(h, u)
+    C = SwComplex(mesh, L, nu=nu)
+    hc, uc = C.step(h, u, dt, n)
+    assert np.abs(hc.ravel() - hr.ravel()).max() <= 1e-13 * np.abs(hr).max()
+    assert np.abs(uc.ravel() - ur.ravel()).max() <= 1e-13 * np.abs(ur).max()
+    rng = np.random.default_rng(0)
+    vh, vu = rng.standard_normal(h.shape), rng.standard_normal(u.shape) * 1e-3
+    jh, ju = C.jvp(h, u, vh, vu, dt, n)
+    eps = 1e-3
+    hp, up, _ = run(h + eps * vh, u + eps * vu)
+    hm, um, _ = run(h - eps * vh, u - eps * vu)
+    fh, fu = (hp - hm) / (2 * eps), (up - um) / (2 * eps)
+    assert np.abs(jh.ravel() - fh.ravel()).max() <= 1e-8 * np.abs(fh).max()
+    assert np.abs(ju.ravel() - fu.ravel()).max() <= 1e-8 * np.abs(fu).max()
