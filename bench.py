@@ -124,6 +124,7 @@ def gpu_arm(args, cfg):
 
     import mpaso.gpu as G
     from mpaso.perfmodel import Dims, ocean_kernels, per_step, sw_kernels
+    from mpaso.replicas import reduce_over_ranks
 
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
@@ -167,10 +168,7 @@ def gpu_arm(args, cfg):
     ms = e0.elapsed_time(e1)
     barrier()
     clocks = sampler.stop()
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = reduce_over_ranks(ms, "max", device="cuda")
     units_rank = mesh.nCells * cfg["L"]
     value = world * units_rank * K / (ms_max * 1e-3)
 
@@ -201,8 +199,11 @@ def gpu_arm(args, cfg):
     fp64 = {"achieved_dfma_per_s": kf / (prof[top] * 1e-3), "peak_dfma_per_s": fp64_peak,
             "frac": round(kf / (prof[top] * 1e-3) / fp64_peak, 4), "kernel": top,
             "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / fp64_peak, 4),
+            "nominal_dfma_per_s": 2.0 * torch.cuda.get_device_properties(local).multi_processor_count
+                                  * (clocks.get("sm_max_mhz") or 2070.0) * 1e6,
             "note": "FP64 instructions per launch from mpaso/perfmodel.py / measured launch time, "
-                    "against the live DFMA issue rate of mpaso_probe_fp64"}
+                    "against the live DFMA issue rate of mpaso_probe_fp64 (independent DFMA chains; "
+                    "the nominal 2 DFMA/clk/SM is not reached by any instruction mix measured)"}
     step_hbm = {"algorithmic_bytes_per_step": int(step_bytes),
                 "achieved_gbs": round(step_bytes / (ms_max * 1e-3 / K) / 1e9, 1),
                 "frac": round(step_bytes / (ms_max * 1e-3 / K) / 1e9 / peak, 4),
@@ -235,10 +236,8 @@ def gpu_arm(args, cfg):
         a1.record(ext)
         a1.synchronize()
         e2e_ms = a0.elapsed_time(a1)
-    t = torch.tensor([e2e_ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    e2e = {"value": world * units_rank * Ke / (float(t.item()) * 1e-3), "unit": "cell-updates/s",
+    e2e_max = reduce_over_ranks(e2e_ms, "max", device="cuda")
+    e2e = {"value": world * units_rank * Ke / (e2e_max * 1e-3), "unit": "cell-updates/s",
            "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
            "path": "mpaso_rk4_step_host (C ABI, pinned host buffers, copy in -> 1 step -> copy out)"
            if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)"}
@@ -370,25 +369,38 @@ def adjoint_arm(args):
 # ---------------------------------------------------------------- ensemble (cfg4)
 def ensemble_arm(args):
     """256 uneven members (192 periodic hex meshes, 64 spheres) advanced as one
-    union, against the same members advanced one at a time."""
+    ensemble context (mpaso_mesh_create_ensemble), against the same members
+    advanced one at a time.  Under torchrun the members are sharded across
+    ranks by cell count (no communication but the timing reduction)."""
     import numpy as np
     import torch
 
+    import mpaso
     import mpaso.gpu as G
-    from mpaso.ensemble import build
     from mpaso.initial import sw_state
+    from mpaso.replicas import reduce_over_ranks, shard
+    from mpaso.setup import fct_statics
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     rng = np.random.default_rng(2024)
     sides = [int(x) for x in args.ens_sides.split(",")]
     levels = [int(x) for x in args.ens_levels.split(",")]
-    specs = [("hex", int(s), int(s), 10e3, 1e-4) for s in rng.choice(sides, args.ens_planar)]
+    specs = [("hex", int(s)) for s in rng.choice(sides, args.ens_planar)]
     specs += [("icosa", int(l)) for l in rng.choice(levels, args.ens_sphere)] if args.ens_sphere else []
+    cells = [s[1] * s[1] if s[0] == "hex" else 10 * 4 ** s[1] + 2 for s in specs]
+    mine = shard(cells, world, rank)
     t0 = time.time()
-    u, fct, offs, members, mfct = build(specs, nlev=1, return_member_fct=True)
-    states = [sw_state(m, 5000 + i, 1, 1) for i, m in enumerate(members)]
-    log(f"ensemble built in {time.time() - t0:.1f}s: {len(members)} members, {u.nCells} cells")
+    members = [mpaso.Mesh.hex(s[1], s[1], 10e3, 1e-4) if s[0] == "hex" else mpaso.Mesh.icosa(s[1])
+               for s in (specs[i] for i in mine)]
+    mfct = [fct_statics(m, 1) for m in members]
+    states = [sw_state(m, 5000 + i, 1, 1) for i, m in zip(mine, members)]
     opts = dict(fct=True, hmix=True, kappa=1e3, nu=1e3)
     dt, K, W = 30.0, args.steps, args.warmup
-    dm = G.DeviceMesh(u, fct=fct, reorder=False)
+    dm = G.DeviceMesh.ensemble(members, mfct, device=local)
+    log(f"ensemble built in {time.time() - t0:.1f}s: {len(members)} members, {dm.nC} cells on rank {rank}")
     st = G.State(dm, nlev=1, ntr=1, **opts)
     for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
         st.set(f, np.concatenate([s[k] for s in states]))
@@ -396,21 +408,23 @@ def ensemble_arm(args):
     launch = st.autotune(dt, 3) if not args.no_autotune else st.launch_config()
     st.step_graph(dt, W)
     st.sync()
+    if world > 1:
+        torch.distributed.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(ext)
     st.step_graph(dt, K)
     e1.record(ext)
     e1.synchronize()
-    t_batch = e0.elapsed_time(e1) * 1e-3
+    t_batch = reduce_over_ranks(e0.elapsed_time(e1) * 1e-3, "max", device="cuda")
     # one member at a time: its own context and graph (same launch shapes),
     # members advanced in turn
     singles = []
     for i, m in enumerate(members):
-        d = G.DeviceMesh(m, fct=mfct[i], reorder=False)
+        d = G.DeviceMesh(m, fct=mfct[i], device=local)
         s = G.State(d, nlev=1, ntr=1, **opts)
         for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
             s.set(f, states[i][k])
-        s.set_launch_config(launch["unroll"], launch["threads"])
+        s.set_launch_config(launch["unroll"], launch["threads"], launch["capped"])  # L2 window: union only
         s.step_graph(dt, W)
         singles.append((d, s))
     torch.cuda.synchronize()
@@ -419,19 +433,33 @@ def ensemble_arm(args):
         s.step_graph(dt, K)
     for d, s in singles:
         s.sync()
-    t_single = time.perf_counter() - t1
-    n = len(members)
-    return {"metric": "ensemble members*steps/s (one graph-captured launch sequence vs one at a time)",
-            "value": n * K / t_batch, "unit": "member-steps/s", "higher_is_better": True, "n_gpus": 1,
-            "steps": K, "warmup": W, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
-            "config": {"workload": f"{args.ens_planar} periodic hex (sides {args.ens_sides}) + {args.ens_sphere} "
-                                   f"sphere (levels {args.ens_levels}) members, sw + FCT tracer + del2, dt={dt}s",
-                       "cells": int(u.nCells), "edges": int(u.nEdges), "members": n, "launch": launch},
-            "cell_updates_per_s": u.nCells * K / t_batch,
-            "one_at_a_time": {"value": n * K / t_single, "unit": "member-steps/s",
-                              "cell_updates_per_s": u.nCells * K / t_single},
-            "speedup_vs_one_at_a_time": t_single / t_batch,
-            "gpu_launches": st.launches_per_step() * K}
+    t_single = reduce_over_ranks(time.perf_counter() - t1, "max", device="cuda")
+    n, ncells = len(specs), sum(cells)
+    out = None
+    if rank == 0:
+        out = {"metric": "ensemble members*steps/s (one graph-captured launch sequence vs one at a time)",
+               "value": n * K / t_batch, "unit": "member-steps/s", "higher_is_better": True, "n_gpus": world,
+               "steps": K, "warmup": W, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
+               "scaling": "strong",
+               "config": {"workload": f"{args.ens_planar} periodic hex (sides {args.ens_sides}) + "
+                                      f"{args.ens_sphere} sphere (levels {args.ens_levels}) members, sw + FCT "
+                                      f"tracer + del2, dt={dt}s",
+                          "cells": int(ncells), "members": n, "launch": launch,
+                          "parallelism": f"members sharded x{world}"},
+               "cell_updates_per_s": ncells * K / t_batch,
+               "one_at_a_time": {"value": n * K / t_single, "unit": "member-steps/s",
+                                 "cell_updates_per_s": ncells * K / t_single},
+               "speedup_vs_one_at_a_time": t_single / t_batch,
+               "gpu_launches": st.launches_per_step() * K}
+    for d, s in singles:
+        s.close()
+        d.close()
+    st.close()
+    dm.close()
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return out
 
 
 # ---------------------------------------------------------------- reference arm

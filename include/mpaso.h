@@ -84,6 +84,22 @@ int mpaso_mesh_set_gravity(mpaso_mesh m, double gravity);
 /* Bytes of device memory held by the context. */
 int mpaso_mesh_device_bytes(mpaso_mesh m, int64_t *bytes);
 
+/* Ensemble of independent members on uneven meshes (no counterpart in the
+ * reference, which runs one mesh): one context over the disjoint union of n
+ * member descriptions, so one state and one graph-captured launch sequence
+ * advance every member.  Reference numbering of the union = the members'
+ * numberings concatenated in member order (fields are set and read as the
+ * concatenation of the members' arrays); with reorder = 1 each member is
+ * renumbered along its own Hilbert curve inside its own block.  Members must
+ * agree on reorder and on having FCT statics (same fct_nlev); they share the
+ * state parameters (dt, gravity, diffusion) and may mix planes and spheres. */
+int mpaso_mesh_create_ensemble(const mpaso_mesh_desc *members, int32_t n, int device,
+                               mpaso_mesh *out);
+/* *n = member count (1 for a plain mesh); offsets (optional, 3 (n + 1)
+ * int64) receive the first cell, edge and vertex of each member, then the
+ * totals. */
+int mpaso_mesh_members(mpaso_mesh m, int32_t *n, int64_t *offsets);
+
 /* ------------------------------------------------------------------------
  * Per-task entries, one per reference task.  Arrays: vlreal [n][L],
  * vltracer [n][L][T], in the reference's numbering.  nlev / ntr are the
@@ -219,21 +235,29 @@ int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per
 int mpaso_state_launches_per_step(mpaso_state s, int32_t *n);
 int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
 
-/* Launch configuration of the three kernels of an RK stage, as 6 ints:
+/* Launch configuration of the three kernels of an RK stage, as 10 ints:
  * config[0..2] = 1 where the kernel's stencil loop is unrolled at compile
  * time (only meaningful where the mesh's widest stencil is 10: the sphere),
- * config[3..5] = threads per block (64, 128 or 256).  Results do not depend
- * on the threads per block; the unrolled and runtime-width variants differ
- * at most in the last bit.  No counterpart in the reference (its tasks have
- * no device launch shape).  Setting it drops any captured step graph. */
+ * config[3..5] = threads per block (64, 128 or 256), config[6..8] = 1 where
+ * the kernel runs with registers capped at 32 per thread for full occupancy
+ * (sw app with at most 2 tracers; otherwise ignored), config[9] = static
+ * array kept resident in the L2 cache's persisting portion (sw app): 0 none,
+ * 1 the FCT advection coefficients, 2 the TRiSK weights.  Results do not
+ * depend on the threads per block or the L2 choice; the other variants may
+ * differ in the last bits.  No counterpart in the reference (its tasks have
+ * no device launch shape).  Setting it drops any captured step graph; a
+ * persisting L2 reservation is per device context, so at most one state per
+ * device should use config[9] != 0, and destroying it releases the
+ * reservation. */
 int mpaso_state_launch_config(mpaso_state s, int32_t *config);
 int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
 /* Per-mesh autotuner: for each stage kernel in turn, times every variant
- * (unrolled or not x 64/128/256 threads) over nsteps steps of size dt and
- * keeps the fastest.  The prognostic state is saved first and restored on
+ * (unrolled or not x capped or not x 64/128/256 threads) over nsteps steps
+ * of size dt and keeps the fastest, then picks the L2 residency choice on
+ * the whole stage.  The prognostic state is saved first and restored on
  * return, so the call leaves (h, u, tracers) unchanged; it allocates one
  * temporary copy of them.  config (may be NULL) receives the chosen
- * configuration.  Call it outside stream capture. */
+ * configuration (10 ints).  Call it outside stream capture. */
 int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config);
 
 /* Adjoint of the sw RK4 step for (h, u).  No counterpart in the reference,

@@ -86,6 +86,8 @@ struct MeshCtx {
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
   void *ensure_scratch(size_t bytes);
+  // ensemble contexts: first cell / edge / vertex of each member (n + 1 rows)
+  std::vector<int64_t> members;
   ~MeshCtx();
 };
 

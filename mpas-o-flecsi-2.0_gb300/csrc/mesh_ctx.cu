@@ -100,7 +100,10 @@ struct Arena {
   }
 };
 
-void build(MeshCtx &ctx, const mpaso_mesh_desc &d) {
+// `mcells` (optional, ensembles): first cell of each member plus the total;
+// members are then renumbered each within its own block, with its own
+// bounding box, so a member keeps the order it would have alone.
+void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *mcells = nullptr) {
   const int64_t nC = d.nCells, nE = d.nEdges, nV = d.nVertices;
   require(nC > 0 && nE > 0 && nV > 0 && nE < (1LL << 30), MPASO_ERR_ARG, "bad entity counts");
   require(d.areaCell && d.dvEdge && d.dcEdge && d.areaTriangle && d.kiteAreasOnVertex && d.fVertex &&
@@ -134,22 +137,33 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d) {
   std::iota(pc.begin(), pc.end(), 0);
   if (d.reorder) {
     require(d.xCell && d.yCell, MPASO_ERR_ARG, "reorder needs xCell/yCell(/zCell)");
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     const double *xyz[3] = {d.xCell, d.yCell, d.zCell};
-    const int dims = d.zCell ? 3 : 2;
-    for (int a = 0; a < dims; ++a)
-      for (int64_t c = 0; c < nC; ++c) lo[a] = std::min(lo[a], xyz[a][c]), hi[a] = std::max(hi[a], xyz[a][c]);
-    const int bits = dims == 3 ? 20 : 30;
+    const std::vector<int64_t> whole = {0, nC};
+    const std::vector<int64_t> &blk = mcells ? *mcells : whole;
     std::vector<uint64_t> key(nC);
-    for (int64_t c = 0; c < nC; ++c) {
-      uint32_t q[3] = {0, 0, 0};
-      for (int a = 0; a < dims; ++a) {
-        const double span = hi[a] > lo[a] ? hi[a] - lo[a] : 1.0;
-        q[a] = (uint32_t)((xyz[a][c] - lo[a]) / span * (double)((1u << bits) - 1));
+    std::vector<int32_t> member(nC, 0);
+    for (size_t b = 0; b + 1 < blk.size(); ++b) {
+      const int64_t c0 = blk[b], c1 = blk[b + 1];
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int a = 0; a < 3; ++a)
+        if (xyz[a])
+          for (int64_t c = c0; c < c1; ++c) lo[a] = std::min(lo[a], xyz[a][c]), hi[a] = std::max(hi[a], xyz[a][c]);
+      // a member whose z is absent or constant (a plane) is ordered in 2-D
+      const int dims = (d.zCell && hi[2] > lo[2]) ? 3 : 2;
+      const int bits = dims == 3 ? 20 : 30;
+      for (int64_t c = c0; c < c1; ++c) {
+        uint32_t q[3] = {0, 0, 0};
+        for (int a = 0; a < dims; ++a) {
+          const double span = hi[a] > lo[a] ? hi[a] - lo[a] : 1.0;
+          q[a] = (uint32_t)((xyz[a][c] - lo[a]) / span * (double)((1u << bits) - 1));
+        }
+        key[c] = hilbert_key(q, dims, bits);
+        member[c] = (int32_t)b;
       }
-      key[c] = hilbert_key(q, dims, bits);
     }
-    std::stable_sort(pc.begin(), pc.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+    std::stable_sort(pc.begin(), pc.end(), [&](int32_t a, int32_t b) {
+      return member[a] != member[b] ? member[a] < member[b] : key[a] < key[b];
+    });
   }
   std::vector<int32_t> ic(nC);
   for (int64_t k = 0; k < nC; ++k) ic[pc[k]] = (int32_t)k;
@@ -336,10 +350,177 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d) {
   }
 }
 
+// Disjoint union of member descriptions: fields concatenated in member
+// order, connectivity and advection-cell indices shifted by each member's
+// first cell / edge / vertex.  The vectors in `keep` own the arrays `u`
+// points at.
+struct Union {
+  mpaso_mesh_desc u{};
+  std::vector<std::vector<int64_t>> offs;
+  std::vector<std::vector<int32_t>> ints;
+  std::vector<std::vector<double>> dbls;
+  std::vector<int64_t> mcells, medges, mverts;
+};
+
+void make_union(Union &U, const mpaso_mesh_desc *m, int n) {
+  require(n >= 1, MPASO_ERR_ARG, "an ensemble needs at least one member");
+  const bool fct = m[0].advCoef != nullptr;
+  U.mcells = {0}, U.medges = {0}, U.mverts = {0};
+  for (int i = 0; i < n; ++i) {
+    require(m[i].nCells > 0 && m[i].nEdges > 0 && m[i].nVertices > 0, MPASO_ERR_ARG, "bad member sizes");
+    require((m[i].advCoef != nullptr) == fct, MPASO_ERR_ARG, "either every member has FCT statics or none");
+    require(!fct || m[i].fct_nlev == m[0].fct_nlev, MPASO_ERR_ARG, "members' FCT statics differ in levels");
+    require((m[i].reorder != 0) == (m[0].reorder != 0), MPASO_ERR_ARG, "members disagree on reorder");
+    U.mcells.push_back(U.mcells.back() + m[i].nCells);
+    U.medges.push_back(U.medges.back() + m[i].nEdges);
+    U.mverts.push_back(U.mverts.back() + m[i].nVertices);
+  }
+  mpaso_mesh_desc &u = U.u;
+  u.nCells = U.mcells.back(), u.nEdges = U.medges.back(), u.nVertices = U.mverts.back();
+  require(u.nEdges < (1LL << 30), MPASO_ERR_ARG, "ensemble too large");
+  // connectivity: (offsets member, index member, rows of member, target offsets)
+  struct C {
+    const int64_t *mpaso_mesh_desc::*off;
+    const int32_t *mpaso_mesh_desc::*idx;
+    const std::vector<int64_t> *rows, *to;
+  };
+  const C cs[5] = {{&mpaso_mesh_desc::c2v_off, &mpaso_mesh_desc::c2v, &U.mcells, &U.mverts},
+                   {&mpaso_mesh_desc::c2e_off, &mpaso_mesh_desc::c2e, &U.mcells, &U.medges},
+                   {&mpaso_mesh_desc::c2c_off, &mpaso_mesh_desc::c2c, &U.mcells, &U.mcells},
+                   {&mpaso_mesh_desc::e2v_off, &mpaso_mesh_desc::e2v, &U.medges, &U.mverts},
+                   {&mpaso_mesh_desc::e2e_off, &mpaso_mesh_desc::e2e, &U.medges, &U.medges}};
+  for (const C &c : cs) {
+    std::vector<int64_t> off = {0};
+    std::vector<int32_t> idx;
+    for (int i = 0; i < n; ++i) {
+      const int64_t *o = m[i].*c.off;
+      const int32_t *x = m[i].*c.idx;
+      require(o && x, MPASO_ERR_ARG, "member connectivity missing");
+      const int64_t rows = (*c.rows)[i + 1] - (*c.rows)[i], shift = (*c.to)[i];
+      const int64_t base = off.back();
+      for (int64_t r = 0; r < rows; ++r) off.push_back(base + o[r + 1]);
+      for (int64_t k = 0; k < o[rows]; ++k) idx.push_back((int32_t)(x[k] + shift));
+    }
+    U.offs.push_back(std::move(off));
+    U.ints.push_back(std::move(idx));
+    u.*c.off = U.offs.back().data();
+    u.*c.idx = U.ints.back().data();
+  }
+  // per-entity fields: (member, values per entity, entity rows, default when NULL)
+  auto cat = [&](const double *mpaso_mesh_desc::*f, int per, const std::vector<int64_t> &rows,
+                 bool may_be_null) -> const double * {
+    std::vector<double> v;
+    v.reserve((size_t)rows.back() * per);
+    for (int i = 0; i < n; ++i) {
+      const double *x = m[i].*f;
+      const int64_t cnt = (rows[i + 1] - rows[i]) * per;
+      require(x || may_be_null, MPASO_ERR_ARG, "member geometry field missing");
+      for (int64_t k = 0; k < cnt; ++k) v.push_back(x ? x[k] : 0.0);
+    }
+    U.dbls.push_back(std::move(v));
+    return U.dbls.back().data();
+  };
+  auto cati = [&](const int32_t *mpaso_mesh_desc::*f, int per, const std::vector<int64_t> &rows) -> const int32_t * {
+    std::vector<int32_t> v;
+    for (int i = 0; i < n; ++i) {
+      const int32_t *x = m[i].*f;
+      require(x, MPASO_ERR_ARG, "member FCT field missing");
+      const int64_t cnt = (rows[i + 1] - rows[i]) * per;
+      for (int64_t k = 0; k < cnt; ++k) v.push_back(x[k]);
+    }
+    U.ints.push_back(std::move(v));
+    return U.ints.back().data();
+  };
+  u.areaCell = cat(&mpaso_mesh_desc::areaCell, 1, U.mcells, false);
+  u.dvEdge = cat(&mpaso_mesh_desc::dvEdge, 1, U.medges, false);
+  u.dcEdge = cat(&mpaso_mesh_desc::dcEdge, 1, U.medges, false);
+  u.areaTriangle = cat(&mpaso_mesh_desc::areaTriangle, 1, U.mverts, false);
+  u.kiteAreasOnVertex = cat(&mpaso_mesh_desc::kiteAreasOnVertex, 3, U.mverts, false);
+  u.fVertex = cat(&mpaso_mesh_desc::fVertex, 1, U.mverts, false);
+  u.weightsOnEdge = cat(&mpaso_mesh_desc::weightsOnEdge, kMaxEdges2, U.medges, false);
+  u.bottomDepth = cat(&mpaso_mesh_desc::bottomDepth, 1, U.mcells, true);
+  u.reorder = m[0].reorder;
+  if (u.reorder) {
+    u.xCell = cat(&mpaso_mesh_desc::xCell, 1, U.mcells, false);
+    u.yCell = cat(&mpaso_mesh_desc::yCell, 1, U.mcells, false);
+    u.zCell = cat(&mpaso_mesh_desc::zCell, 1, U.mcells, true);
+  }
+  if (fct) {
+    const int L = m[0].fct_nlev;
+    u.fct_nlev = L;
+    u.maxLevelCell = cati(&mpaso_mesh_desc::maxLevelCell, 1, U.mcells);
+    u.maxLevelEdgeTop = cati(&mpaso_mesh_desc::maxLevelEdgeTop, 1, U.medges);
+    u.nAdvCellsForEdge = cati(&mpaso_mesh_desc::nAdvCellsForEdge, 1, U.medges);
+    u.highOrderAdvMask = cati(&mpaso_mesh_desc::highOrderAdvMask, L, U.medges);
+    // advection cells: the first nAdv entries of each row shift by the member's first cell
+    std::vector<int32_t> adv;
+    adv.reserve((size_t)u.nEdges * kMaxEdges2);
+    for (int i = 0; i < n; ++i) {
+      require(m[i].advCellsForEdge && m[i].nAdvCellsForEdge, MPASO_ERR_ARG, "member FCT field missing");
+      for (int64_t e = 0; e < m[i].nEdges; ++e)
+        for (int j = 0; j < kMaxEdges2; ++j) {
+          const int32_t x = m[i].advCellsForEdge[e * kMaxEdges2 + j];
+          adv.push_back(j < m[i].nAdvCellsForEdge[e] ? (int32_t)(x + U.mcells[i]) : x);
+        }
+    }
+    U.ints.push_back(std::move(adv));
+    u.advCellsForEdge = U.ints.back().data();
+    u.edgeSignOnCell = cat(&mpaso_mesh_desc::edgeSignOnCell, kMaxEdges, U.mcells, false);
+    u.advCoef = cat(&mpaso_mesh_desc::advCoef, kMaxEdges2, U.medges, false);
+    u.advCoef_3rd = cat(&mpaso_mesh_desc::advCoef_3rd, kMaxEdges2, U.medges, false);
+    u.meshScalingDel2 = cat(&mpaso_mesh_desc::meshScalingDel2, 1, U.medges, false);
+  }
+}
+
 }  // namespace
 }  // namespace mpaso
 
 extern "C" {
+
+int mpaso_mesh_create_ensemble(const mpaso_mesh_desc *members, int32_t n, int device, mpaso_mesh *out) {
+  return mpaso::guarded("mpaso_mesh_create_ensemble", [&] {
+    mpaso::require(members && out && n >= 1, MPASO_ERR_ARG, "bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      mpaso::fail(MPASO_ERR_NODEVICE, "no CUDA device");
+    }
+    if (device < 0) MPASO_CUDA(cudaGetDevice(&device));
+    mpaso::require(device < ndev, MPASO_ERR_ARG, "device index out of range");
+    MPASO_CUDA(cudaSetDevice(device));
+    mpaso::Union U;
+    mpaso::make_union(U, members, n);
+    auto *h = new mpaso_mesh_s();
+    try {
+      h->ctx.device = device;
+      MPASO_CUDA(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking));
+      mpaso::build(h->ctx, U.u, &U.mcells);
+      for (int i = 0; i <= n; ++i)
+        h->ctx.members.insert(h->ctx.members.end(), {U.mcells[i], U.medges[i], U.mverts[i]});
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int mpaso_mesh_members(mpaso_mesh m, int32_t *n, int64_t *offsets) {
+  return mpaso::guarded("mpaso_mesh_members", [&] {
+    mpaso::require(m && n, MPASO_ERR_ARG, "null argument");
+    const auto &mb = m->ctx.members;
+    if (mb.empty()) {  // a plain mesh is an ensemble of one
+      *n = 1;
+      if (offsets) {
+        const int64_t v[6] = {0, 0, 0, m->ctx.d.nC, m->ctx.d.nE, m->ctx.d.nV};
+        std::memcpy(offsets, v, sizeof v);
+      }
+      return;
+    }
+    *n = (int32_t)(mb.size() / 3 - 1);
+    if (offsets) std::memcpy(offsets, mb.data(), mb.size() * sizeof(int64_t));
+  });
+}
 
 int mpaso_device_count(int32_t *n) {
   return mpaso::guarded("mpaso_device_count", [&] {

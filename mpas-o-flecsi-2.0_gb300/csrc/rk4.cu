@@ -30,11 +30,17 @@ namespace mpaso {
 namespace {
 
 constexpr int TPB = 256;
-// ------------------------------------------------------------- K1: edges
+// Launch-shape variants of the stage kernels (picked per mesh by the autotuner):
 // NW = 10: edgesOnEdge and advection stencils of exactly 10 slots (hexagon /
 // pentagon meshes), unrolled at compile time; NW = 0: runtime widths.
-template <int T, int NW>
-__global__ void __launch_bounds__(TPB) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
+// OC = 1: registers capped at 32 so 2048 threads fit an SM (more warps to hide
+// gather latency, less ILP per warp); OC = 0: the compiler's choice.
+constexpr int kOccMaxT = 2;  // OC = 1 variants exist up to this many tracers
+#define MPASO_BOUNDS(OC) __launch_bounds__(TPB, (OC) ? 2048 / TPB : 1)
+
+// ------------------------------------------------------------- K1: edges
+template <int T, int NW, int OC>
+__global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
@@ -51,8 +57,8 @@ __global__ void __launch_bounds__(TPB) k_sw_edge_pre(DMesh m, DStat st, Stage S,
 }
 
 // ------------------------------------------------------ K2: edges + cells
-template <int T, int NW>
-__global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
+template <int T, int NW, int OC>
+__global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nEL = (int64_t)m.nE * L;
   if (i < nEL) {
@@ -71,11 +77,11 @@ __global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int
     const double q = fma(S.pve[i], s1, s2);
     const int2 c = m.coe[e];
     const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-    const double dh = (S.h_in[i2] - S.h_in[i1]) + st.dhs[e];
-    double tend = fma(-m.invDcEdge[e], fma(S.g, dh, S.ke[i2] - S.ke[i1]), q);
-    if (S.visc) {  // + nu ((div2 - div1) / dc - (vort_b - vort_a) / dv)
+    // - (ke2 - ke1 + g (h2 + b2 - h1 - b1)) / dc + nu (div2 - div1) / dc as one
+    // gradient of the cell function bern = ke + g (h + b) - nu div
+    double tend = fma(-m.invDcEdge[e], S.bern[i2] - S.bern[i1], q);
+    if (S.visc) {  // - nu (vort_b - vort_a) / dv
       const int2 v = m.voe[e];
-      tend = fma(st.nuDc[e], S.divc[i2] - S.divc[i1], tend);
       tend = fma(-st.nuDv[e], S.vort[(int64_t)v.y * L + k] - S.vort[(int64_t)v.x * L + k], tend);
     }
     const double up = S.u_prev[i];
@@ -123,9 +129,12 @@ __global__ void __launch_bounds__(TPB) k_sw_tend(DMesh m, DStat st, Stage S, int
   }
 }
 
-// Diagnostics of a state (u, h): ke, div at cells; vorticity, pv at vertices.
+// Diagnostics of a state (u, h): at cells the Bernoulli-type function
+// bern = ke + g (h + b) - nu div whose edge difference / dcEdge is the whole
+// gradient part of tend_u (apps/sw/tasks/solve.cc:228-231 plus del2
+// momentum); vorticity and pv at vertices.
 __device__ __forceinline__ void cell_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
-                                          int c, int k, int64_t i, const double *u) {
+                                          int c, int k, int64_t i, const double *u, double h) {
   const int n = m.nEoC[c];
   double ke = 0.0, dv = 0.0;
   for (int j = 0; j < n; ++j) {
@@ -134,10 +143,10 @@ __device__ __forceinline__ void cell_diag(const DMesh &m, const DStat &st, const
     ke = fma(st.kw[e], ue * ue, ke);
     if (S.visc) dv = fma(st.sdv[(int64_t)j * m.nC + c], ue, dv);
   }
-  const double inva = m.invAreaCell[c];
-  S.ke[i] = ke * inva;
-  // sdv = edgeSignOnCell dv is inward-positive; the divergence is outward-positive
-  if (S.visc) S.divc[i] = -dv * inva;
+  double b = fma(S.g, h, fma(ke, m.invAreaCell[c], st.gbd[c]));
+  // sdv = edgeSignOnCell dv is inward-positive: div = -dv / area, -nu div = nu dv / area
+  if (S.visc) b = fma(st.nuInva[c], dv, b);
+  S.bern[i] = b;
 }
 
 __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
@@ -156,18 +165,19 @@ __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, con
 }
 
 // ------------------------------------------------------ K3: cells + vertices
-template <int T>
-__global__ void __launch_bounds__(TPB) k_sw_final(DMesh m, DStat st, Stage S, int L) {
+template <int T, int OC>
+__global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
   const double *u_next = S.stage == 3 ? S.u_new : S.u_out;
   const double *h_next = S.stage == 3 ? S.h_new : S.h_out;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+    const double hn = h_next[i];
     if constexpr (T > 0) {
       double tend[T];
       cell_tracer_tend<T>(m, S, L, c, k, i, tend);
-      const double rh = rcp_nr(h_next[i]);
+      const double rh = rcp_nr(hn);
       const double hpv = S.h_prev[i];
 #pragma unroll
       for (int t = 0; t < T; ++t) {
@@ -187,7 +197,7 @@ __global__ void __launch_bounds__(TPB) k_sw_final(DMesh m, DStat st, Stage S, in
         }
       }
     }
-    cell_diag(m, st, S, L, c, k, i, u_next);
+    cell_diag(m, st, S, L, c, k, i, u_next, hn);
     return;
   }
   i -= nCL;
@@ -202,7 +212,7 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    cell_diag(m, st, S, L, c, k, i, S.u_in);
+    cell_diag(m, st, S, L, c, k, i, S.u_in, S.h_in[i]);
     return;
   }
   i -= nCL;
@@ -213,12 +223,12 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
 
 // Derived statics of a state.
 struct StatOut {
-  double *sdv, *sdvi, *kw, *sdc, *dhs, *kd, *kdh, *dvh, *woe8;
+  double *sdv, *sdvi, *kw, *sdc, *gbd, *kd, *kdh, *dvh, *woe8;
   double2 *cpm2, *cpm1;
-  double *nuDc, *nuDv;
+  double *nuInva, *nuDv;
 };
 
-__global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
+__global__ void k_build_stat(DMesh m, double g, double kappa, double nu, StatOut o) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < (int64_t)m.maxEoC * m.nC) {
     const int c = (int)(i % m.nC), j = (int)(i / m.nC);
@@ -226,15 +236,16 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
     o.sdv[i] = s;
     o.sdvi[i] = 0.5 * s * m.invAreaCell[c];
   }
+  if (i < m.nC) {
+    o.gbd[i] = g * m.bottomDepth[i];
+    o.nuInva[i] = nu * m.invAreaCell[i];
+  }
   if (i < m.nE) {
     o.kw[i] = 0.25 * m.dcEdge[i] * m.dvEdge[i];
-    const int2 c = m.coe[i];
-    o.dhs[i] = m.bottomDepth[c.y] - m.bottomDepth[c.x];
     const double kd = m.meshScalingDel2[i] * kappa * m.dvEdge[i] * m.invDcEdge[i];
     o.kd[i] = kd;
     o.kdh[i] = 0.5 * kd;
     o.dvh[i] = 0.5 * m.dvEdge[i];
-    o.nuDc[i] = nu * m.invDcEdge[i];
     o.nuDv[i] = nu * m.invDvEdge[i];
   }
   if (i < (int64_t)m.maxEoE * m.nE) o.woe8[i] = 0.125 * m.woe[i];
@@ -250,6 +261,10 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
 // ------------------------------------------------------------ state context
 SwState::~SwState() {
   if (graph) cudaGraphExecDestroy(graph);
+  if (tune_l2) {  // hand the persisting L2 lines back
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+  }
   free_adjoint(*this);
   if (arena) cudaFree(arena);
 }
@@ -276,10 +291,10 @@ void build_stat(SwState &s) {
   const int64_t nmax2 = std::max<int64_t>(nmax, std::max<int64_t>((int64_t)m.maxEoE * m.nE,
                                                                   (int64_t)m.maxAdv * m.nE));
   StatOut o{(double *)s.st.sdv, (double *)s.st.sdvi, (double *)s.st.kw, (double *)s.st.sdc,
-            (double *)s.st.dhs, (double *)s.st.kd, (double *)s.st.kdh, (double *)s.st.dvh,
-            (double *)s.st.woe8, (double2 *)s.st.cpm2, (double2 *)s.st.cpm1, (double *)s.st.nuDc,
+            (double *)s.st.gbd, (double *)s.st.kd, (double *)s.st.kdh, (double *)s.st.dvh,
+            (double *)s.st.woe8, (double2 *)s.st.cpm2, (double2 *)s.st.cpm1, (double *)s.st.nuInva,
             (double *)s.st.nuDv};
-  k_build_stat<<<blocks_for(nmax2, TPB), TPB, 0, s.stream>>>(m, s.p.kappa, s.p.nu, o);
+  k_build_stat<<<blocks_for(nmax2, TPB), TPB, 0, s.stream>>>(m, s.p.gravity, s.p.kappa, s.p.nu, o);
   MPASO_CUDA(cudaGetLastError());
 }
 
@@ -290,10 +305,10 @@ void stat_buffers(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs) 
   DStat &t = s.st;
   auto P = [](const double *&p) { return (double **)&p; };
   bufs.insert(bufs.end(), {{P(t.sdv), (int64_t)m.maxEoC * nC}, {P(t.sdvi), (int64_t)m.maxEoC * nC},
-                           {P(t.kw), nE}, {P(t.sdc), 3 * nV}, {P(t.dhs), nE}, {P(t.kd), nE},
+                           {P(t.kw), nE}, {P(t.sdc), 3 * nV}, {P(t.gbd), nC}, {P(t.kd), nE},
                            {P(t.kdh), nE}, {P(t.dvh), nE}, {P(t.woe8), (int64_t)m.maxEoE * nE},
                            {(double **)&t.cpm2, 2LL * m.maxAdv * nE},
-                           {(double **)&t.cpm1, 2LL * m.maxAdv * nE}, {P(t.nuDc), nE}, {P(t.nuDv), nE}});
+                           {(double **)&t.cpm1, 2LL * m.maxAdv * nE}, {P(t.nuInva), nC}, {P(t.nuDv), nE}});
 }
 
 namespace {
@@ -315,29 +330,78 @@ Stage make_stage(SwState &s, int rk, double dt) {
   S.tr_out = rk < 3 ? trs[rk + 1] : nullptr;
   S.u_acc = s.U[2], S.h_acc = s.H[2], S.trh_acc = s.TRH;
   S.u_new = s.U[0], S.h_new = s.H[0], S.tr_new = s.TR0;
-  S.pv = s.pv, S.vort = s.vort, S.ke = s.ke, S.divc = s.divc;
+  S.pv = s.pv, S.vort = s.vort, S.bern = s.bern;
   S.F = s.F, S.G = s.G, S.pve = s.pve, S.A = s.A, S.LO = s.LO, S.DF = s.DF;
   S.Rp = s.Rp, S.Rm = s.Rm, S.tLO = s.tLO;
   return S;
 }
 
+// Launch of a stage kernel, with the state's L2 persistence window attached
+// when `win` (the window then travels into captured graphs with the launch).
+template <class... A>
+void launch_ex(void (*kern)(A...), int64_t n, int b, bool win, const SwState &s, cudaStream_t st,
+               DMesh m, DStat d, Stage S, int L) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks_for(n, b));
+  cfg.blockDim = dim3(b);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  if (win) {
+    at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    at[0].val.accessPolicyWindow = s.l2win;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  MPASO_CUDA(cudaLaunchKernelEx(&cfg, kern, m, d, S, L));
+}
+
+template <int T, int OC>
+void launch_k1(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t n = (int64_t)m.nE * s.L;
+  const bool win = s.tune_l2 == 1;
+  if (unroll)
+    launch_ex(k_sw_edge_pre<T, 10, OC>, n, b, win, s, st, m, s.st, S, s.L);
+  else
+    launch_ex(k_sw_edge_pre<T, 0, OC>, n, b, win, s, st, m, s.st, S, s.L);
+}
+
+template <int T, int OC>
+void launch_k2(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t n = ((int64_t)m.nE + m.nC) * s.L;
+  const bool win = s.tune_l2 == 2;
+  if (unroll)
+    launch_ex(k_sw_tend<T, 10, OC>, n, b, win, s, st, m, s.st, S, s.L);
+  else
+    launch_ex(k_sw_tend<T, 0, OC>, n, b, win, s, st, m, s.st, S, s.L);
+}
+
+template <int T, int OC>
+void launch_k3(const SwState &s, const Stage &S, int b, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  k_sw_final<T, OC><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, b), b, 0, st>>>(m, s.st, S, s.L);
+}
+
 template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
-  const int L = s.L;
   cudaEvent_t *ev = s.prof_events;
   const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0);
-  const int b0 = s.tune_tpb[0], b1 = s.tune_tpb[1], b2 = s.tune_tpb[2];
-  if (w10 && s.tune_unroll[0])
-    k_sw_edge_pre<T, 10><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
+  constexpr int OC1 = T <= kOccMaxT ? 1 : 0;  // no capped variants compiled beyond kOccMaxT
+  if (OC1 && s.tune_occ[0])
+    launch_k1<T, OC1>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
   else
-    k_sw_edge_pre<T, 0><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
+    launch_k1<T, 0>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
-  if (w10 && s.tune_unroll[1])
-    k_sw_tend<T, 10><<<blocks_for(((int64_t)m.nE + m.nC) * L, b1), b1, 0, st>>>(m, s.st, S, L);
+  if (OC1 && s.tune_occ[1])
+    launch_k2<T, OC1>(s, S, w10 && s.tune_unroll[1], s.tune_tpb[1], st);
   else
-    k_sw_tend<T, 0><<<blocks_for(((int64_t)m.nE + m.nC) * L, b1), b1, 0, st>>>(m, s.st, S, L);
+    launch_k2<T, 0>(s, S, w10 && s.tune_unroll[1], s.tune_tpb[1], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
-  k_sw_final<T><<<blocks_for(((int64_t)m.nC + m.nV) * L, b2), b2, 0, st>>>(m, s.st, S, L);
+  if (OC1 && s.tune_occ[2])
+    launch_k3<T, OC1>(s, S, s.tune_tpb[2], st);
+  else
+    launch_k3<T, 0>(s, S, s.tune_tpb[2], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
@@ -389,7 +453,7 @@ void sw_create(SwState &s) {
       {&s.U[0], nE * L}, {&s.U[1], nE * L}, {&s.U[2], nE * L}, {&s.U[3], nE * L},
       {&s.H[0], nC * L}, {&s.H[1], nC * L}, {&s.H[2], nC * L}, {&s.H[3], nC * L},
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
-      {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.ke, nC * L}, {&s.divc, nC * L},
+      {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.bern, nC * L},
       {&s.F, nE * L}, {&s.G, nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
       {&s.DF, nE * L * T}, {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T}};
   stat_buffers(s, bufs);
@@ -498,6 +562,53 @@ bool has_unrolled(const SwState &S, int k) {
   const DMesh &m = S.mesh->ctx.d;
   if (S.p.app == MPASO_APP_OCEAN) return k == 0 && m.maxAdv == 10;
   return k < 2 && m.maxEoE == 10 && (m.maxAdv == 10 || !S.p.fct || S.T == 0);
+}
+
+// Whether the register-capped (full occupancy) variants exist for this state.
+bool has_capped(const SwState &S) { return S.p.app == MPASO_APP_SW && S.T <= kOccMaxT; }
+
+// The static array an L2 window choice makes persistent, and its bytes.
+std::pair<const void *, size_t> l2_target(const SwState &S, int which) {
+  const DMesh &m = S.mesh->ctx.d;
+  if (S.p.app != MPASO_APP_SW) return {nullptr, 0};
+  if (which == 1 && S.p.fct && S.T > 0) return {S.st.cpm2, (size_t)m.maxAdv * m.nE * sizeof(double2)};
+  if (which == 2) return {S.st.woe8, (size_t)m.maxEoE * m.nE * sizeof(double)};
+  return {nullptr, 0};
+}
+
+// Sets the state's L2 persistence choice: reserves the device's persisting
+// L2 (up to its maximum) and builds the access-policy window the chosen
+// kernel's launches carry.  `which` = 0 releases it.
+void set_l2_window(SwState &S, int which) {
+  const int dev = S.mesh->ctx.device;
+  const auto t = l2_target(S, which);
+  if (!t.first) which = 0;
+  if (S.tune_l2 && !which) {
+    MPASO_CUDA(cudaCtxResetPersistingL2Cache());
+    MPASO_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0));
+  }
+  S.tune_l2 = which;
+  S.l2win = cudaAccessPolicyWindow{};
+  if (!which) return;
+  int maxp = 0, maxw = 0;
+  MPASO_CUDA(cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev));
+  MPASO_CUDA(cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev));
+  require(maxp > 0 && maxw > 0, MPASO_ERR_ARG, "device has no persisting L2");
+  const size_t bytes = std::min(t.second, (size_t)maxw);
+  const size_t aside = std::min(bytes, (size_t)maxp);
+  MPASO_CUDA(cudaCtxResetPersistingL2Cache());
+  MPASO_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, aside));
+  S.l2win.base_ptr = const_cast<void *>(t.first);
+  S.l2win.num_bytes = bytes;
+  S.l2win.hitRatio = (float)std::min(1.0, (double)aside / (double)bytes);
+  S.l2win.hitProp = cudaAccessPropertyPersisting;
+  S.l2win.missProp = cudaAccessPropertyStreaming;
+}
+
+void get_config(const SwState &S, int32_t *config) {
+  for (int k = 0; k < 3; ++k)
+    config[k] = S.tune_unroll[k], config[3 + k] = S.tune_tpb[k], config[6 + k] = S.tune_occ[k];
+  config[9] = S.tune_l2;
 }
 
 constexpr int kTpbChoices[3] = {64, 128, 256};
@@ -701,7 +812,7 @@ int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes) {
 int mpaso_state_launch_config(mpaso_state s, int32_t *config) {
   return guarded("mpaso_state_launch_config", [&] {
     require(s && config, MPASO_ERR_ARG, "null argument");
-    for (int k = 0; k < 3; ++k) config[k] = s->s.tune_unroll[k], config[3 + k] = s->s.tune_tpb[k];
+    get_config(s->s, config);
   });
 }
 
@@ -712,12 +823,16 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
       require(config[k] == 0 || config[k] == 1, MPASO_ERR_ARG, "unroll flag must be 0 or 1");
       const int b = config[3 + k];
       require(b == 64 || b == 128 || b == 256, MPASO_ERR_ARG, "threads per block must be 64, 128 or 256");
+      require(config[6 + k] == 0 || config[6 + k] == 1, MPASO_ERR_ARG, "occupancy flag must be 0 or 1");
     }
+    require(config[9] >= 0 && config[9] <= 2, MPASO_ERR_ARG, "L2 window choice must be 0, 1 or 2");
     SwState &S = s->s;
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
     drop_graph(S);
-    for (int k = 0; k < 3; ++k) S.tune_unroll[k] = config[k], S.tune_tpb[k] = config[3 + k];
+    for (int k = 0; k < 3; ++k)
+      S.tune_unroll[k] = config[k], S.tune_tpb[k] = config[3 + k], S.tune_occ[k] = config[6 + k];
+    set_l2_window(S, config[9]);
   });
 }
 
@@ -754,16 +869,34 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
       time_stage_kernels(S, dt, 1, ms);  // warm-up
       for (int k = 0; k < 3; ++k) {
         double best = 1e300;
-        int best_u = S.tune_unroll[k], best_b = S.tune_tpb[k];
+        int best_u = S.tune_unroll[k], best_b = S.tune_tpb[k], best_o = S.tune_occ[k];
         for (int u = has_unrolled(S, k) ? 1 : 0; u >= 0; --u)
-          for (int b : kTpbChoices) {
-            S.tune_unroll[k] = u, S.tune_tpb[k] = b;
-            save_restore(false);
-            time_stage_kernels(S, dt, nsteps, ms);
-            if (ms[k] < best) best = ms[k], best_u = u, best_b = b;
-          }
-        S.tune_unroll[k] = best_u, S.tune_tpb[k] = best_b;
+          for (int o = 0; o <= (has_capped(S) ? 1 : 0); ++o)
+            for (int b : kTpbChoices) {
+              S.tune_unroll[k] = u, S.tune_tpb[k] = b, S.tune_occ[k] = o;
+              // one untimed step first: a variant's first launch loads its code
+              save_restore(false);
+              time_stage_kernels(S, dt, 1, ms);
+              save_restore(false);
+              time_stage_kernels(S, dt, nsteps, ms);
+              if (ms[k] < best) best = ms[k], best_u = u, best_b = b, best_o = o;
+            }
+        S.tune_unroll[k] = best_u, S.tune_tpb[k] = best_b, S.tune_occ[k] = best_o;
       }
+      // L2 persistence changes every kernel's hit rate: judged on the whole stage
+      double best = 1e300;
+      int best_l2 = 0;
+      for (int w = 0; w <= 2; ++w) {
+        if (w && !l2_target(S, w).first) continue;
+        set_l2_window(S, w);
+        save_restore(false);
+        time_stage_kernels(S, dt, 1, ms);
+        save_restore(false);
+        time_stage_kernels(S, dt, nsteps, ms);
+        const double tot = ms[0] + ms[1] + ms[2];
+        if (tot < 0.98 * best) best = tot, best_l2 = w;  // keep the simpler choice unless clearly faster
+      }
+      set_l2_window(S, best_l2);
       save_restore(false);
       MPASO_CUDA(cudaStreamSynchronize(S.stream));
     } catch (...) {
@@ -772,8 +905,7 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
       throw;
     }
     MPASO_CUDA(cudaFree(keep));
-    if (config)
-      for (int k = 0; k < 3; ++k) config[k] = S.tune_unroll[k], config[3 + k] = S.tune_tpb[k];
+    if (config) get_config(S, config);
   });
 }
 

@@ -34,7 +34,7 @@ struct DStat {
   const double *sdvi;  // [maxEoC][nC] 0.5 * edgeSignOnCell * dvEdge / areaCell (tend_h from F2)
   const double *kw;    // [nE] 0.25 * dcEdge * dvEdge
   const double *sdc;   // [3][nV] circulation sign * dcEdge
-  const double *dhs;   // [nE] h_s(c2) - h_s(c1)
+  const double *gbd;   // [nC] gravity * bottomDepth
   const double *kd;    // [nE] meshScalingDel2 * kappa * dvEdge / dcEdge
   const double *kdh;   // [nE] kd / 2 (del2 flux from h1 + h2)
   const double *dvh;   // [nE] dvEdge / 2 (fluxes from F2)
@@ -43,7 +43,8 @@ struct DStat {
   // (cpm2, sw kernels) or not (cpm1, ocean kernels); one 16-byte load per slot, the
   // flux sign picks the member.
   const double2 *cpm2, *cpm1;
-  const double *nuDc, *nuDv;  // [nE] nu / dcEdge, nu / dvEdge
+  const double *nuInva;  // [nC] nu / areaCell
+  const double *nuDv;    // [nE] nu / dvEdge
 };
 
 // One RK stage's pointers and weights.
@@ -57,7 +58,7 @@ struct Stage {
   double *u_out, *h_out, *tr_out;           // next stage input (stages 0..2)
   double *u_acc, *h_acc, *trh_acc;          // RK accumulators
   double *u_new, *h_new, *tr_new;           // step result (stage 3)
-  double *pv, *vort, *ke, *divc;            // diagnostics of the stage input
+  double *pv, *vort, *bern;                 // diagnostics of the stage input
   double *F, *G, *pve, *A, *LO, *DF;        // edge intermediates
   double *Rp, *Rm, *tLO;                    // cell intermediates
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
@@ -73,7 +74,7 @@ struct SwState {
   size_t arena_bytes = 0;
   double *U[4]{}, *H[4]{}, *TR0 = nullptr, *TRA = nullptr, *TRB = nullptr, *TRH = nullptr;
   double *HE = nullptr, *HPI = nullptr;
-  double *pv = nullptr, *vort = nullptr, *ke = nullptr, *divc = nullptr;
+  double *pv = nullptr, *vort = nullptr, *bern = nullptr;
   double *F = nullptr, *G = nullptr, *pve = nullptr, *A = nullptr, *LO = nullptr, *DF = nullptr;
   double *Rp = nullptr, *Rm = nullptr, *tLO = nullptr;
   DStat st{};
@@ -86,9 +87,16 @@ struct SwState {
   // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu
   struct AdjBuffers *adj = nullptr;
   // launch configuration of the three stage kernels (autotuned): stencil
-  // unrolled at compile time (1) or runtime width (0), threads per block
+  // unrolled at compile time (1) or runtime width (0), threads per block, and
+  // registers capped for full occupancy (1) or not (0)
   int tune_unroll[3] = {1, 1, 1};
   int tune_tpb[3] = {256, 256, 256};
+  int tune_occ[3] = {0, 0, 0};
+  // L2 residency of one static array across the step: 0 none, 1 the advection
+  // coefficient pairs (read by K1), 2 the TRiSK weights (read by K2); the
+  // window is attached to that kernel's launches (see set_l2_window)
+  int tune_l2 = 0;
+  cudaAccessPolicyWindow l2win{};
   ~SwState();
 };
 

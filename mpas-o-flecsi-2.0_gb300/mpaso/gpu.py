@@ -73,42 +73,76 @@ def device_count():
     return n.value
 
 
+def _mesh_desc(mesh, fct, bottomDepth, reorder, keep):
+    """mpaso_mesh_desc of a generated mesh; the arrays it points at go into `keep`."""
+    crs = mesh.crs()
+    f = mesh.fields
+
+    def arr(a, dtype):
+        a = np.ascontiguousarray(a, dtype)
+        keep.append(a)
+        return _np_ptr(a, _dp if dtype == np.float64 else (_ip if dtype == np.int32 else _lp))
+
+    d = MeshDesc()
+    d.nCells, d.nEdges, d.nVertices = mesh.nCells, mesh.nEdges, mesh.nVertices
+    for n in ("c2v", "c2e", "c2c", "e2v", "e2e"):
+        off, idx = crs[n]
+        setattr(d, n + "_off", arr(off, np.int64))
+        setattr(d, n, arr(idx, np.int32))
+    for n in ("areaCell", "dvEdge", "dcEdge", "areaTriangle", "kiteAreasOnVertex", "fVertex",
+              "weightsOnEdge", "xCell", "yCell", "zCell"):
+        setattr(d, n, arr(f[n], np.float64))
+    if bottomDepth is not None:
+        d.bottomDepth = arr(bottomDepth, np.float64)
+    d.reorder = 1 if reorder else 0
+    if fct is not None:
+        d.fct_nlev = fct["highOrderAdvMask"].shape[1]
+        for n in ("maxLevelCell", "maxLevelEdgeTop", "nAdvCellsForEdge", "advCellsForEdge",
+                  "highOrderAdvMask"):
+            setattr(d, n, arr(fct[n], np.int32))
+        for n in ("edgeSignOnCell", "advCoef", "advCoef_3rd", "meshScalingDel2"):
+            setattr(d, n, arr(fct[n], np.float64))
+    return d
+
+
 class DeviceMesh:
     """Device mesh context built from a generated mpaso.Mesh (reference semantics)."""
 
     def __init__(self, mesh, fct=None, bottomDepth=None, reorder=True, device=0):
-        crs = mesh.crs()
-        f = mesh.fields
-        keep = {}
-
-        def arr(name, a, dtype):
-            a = np.ascontiguousarray(a, dtype)
-            keep[name] = a
-            return _np_ptr(a, _dp if dtype == np.float64 else (_ip if dtype == np.int32 else _lp))
-
-        d = MeshDesc()
-        d.nCells, d.nEdges, d.nVertices = mesh.nCells, mesh.nEdges, mesh.nVertices
-        for n in ("c2v", "c2e", "c2c", "e2v", "e2e"):
-            off, idx = crs[n]
-            setattr(d, n + "_off", arr(n + "_off", off, np.int64))
-            setattr(d, n, arr(n, idx, np.int32))
-        for n in ("areaCell", "dvEdge", "dcEdge", "areaTriangle", "kiteAreasOnVertex", "fVertex",
-                  "weightsOnEdge", "xCell", "yCell", "zCell"):
-            setattr(d, n, arr(n, f[n], np.float64))
-        if bottomDepth is not None:
-            d.bottomDepth = arr("bottomDepth", bottomDepth, np.float64)
-        d.reorder = 1 if reorder else 0
-        if fct is not None:
-            d.fct_nlev = fct["highOrderAdvMask"].shape[1]
-            for n in ("maxLevelCell", "maxLevelEdgeTop", "nAdvCellsForEdge", "advCellsForEdge",
-                      "highOrderAdvMask"):
-                setattr(d, n, arr(n, fct[n], np.int32))
-            for n in ("edgeSignOnCell", "advCoef", "advCoef_3rd", "meshScalingDel2"):
-                setattr(d, n, arr(n, fct[n], np.float64))
+        if mesh is None:  # filled in by a classmethod
+            return
+        keep = []
+        d = _mesh_desc(mesh, fct, bottomDepth, reorder, keep)
         self._h = ctypes.c_void_p()
         check(lib().mpaso_mesh_create(ctypes.byref(d), int(device), ctypes.byref(self._h)))
         self.mesh = mesh
         self.nC, self.nE, self.nV = mesh.nCells, mesh.nEdges, mesh.nVertices
+
+    @classmethod
+    def ensemble(cls, meshes, fcts=None, bottomDepths=None, reorder=True, device=0):
+        """One context over the disjoint union of the member meshes
+        (mpaso_mesh_create_ensemble); fields are the members' concatenated."""
+        keep = []
+        descs = (MeshDesc * len(meshes))()
+        for i, m in enumerate(meshes):
+            descs[i] = _mesh_desc(m, None if fcts is None else fcts[i],
+                                  None if bottomDepths is None else bottomDepths[i], reorder, keep)
+        self = cls(None)
+        self._h = ctypes.c_void_p()
+        check(lib().mpaso_mesh_create_ensemble(descs, len(meshes), int(device), ctypes.byref(self._h)))
+        self.mesh = None
+        self.nC = sum(m.nCells for m in meshes)
+        self.nE = sum(m.nEdges for m in meshes)
+        self.nV = sum(m.nVertices for m in meshes)
+        return self
+
+    def members(self):
+        """(n + 1, 3) int64: first cell, edge, vertex of each member, then the totals."""
+        n = ctypes.c_int32()
+        check(lib().mpaso_mesh_members(self._h, ctypes.byref(n), None))
+        out = np.empty((n.value + 1, 3), np.int64)
+        check(lib().mpaso_mesh_members(self._h, ctypes.byref(n), _np_ptr(out, _lp)))
+        return out
 
     def close(self):
         if getattr(self, "_h", None):
@@ -247,22 +281,24 @@ class State:
     # ---- launch configuration of the three stage kernels ----
     @staticmethod
     def _cfg_dict(c):
-        return {"unroll": [int(x) for x in c[:3]], "threads": [int(x) for x in c[3:]]}
+        return {"unroll": [int(x) for x in c[:3]], "threads": [int(x) for x in c[3:6]],
+                "capped": [int(x) for x in c[6:9]], "l2": int(c[9])}
 
     def launch_config(self):
-        """{'unroll': [3 flags], 'threads': [3 block sizes]} of the stage kernels."""
-        c = (ctypes.c_int32 * 6)()
+        """{'unroll', 'threads', 'capped'}: one value per stage kernel; 'l2': the
+        static array kept resident in L2 (0 none, 1 advection coefficients, 2 TRiSK weights)."""
+        c = (ctypes.c_int32 * 10)()
         check(lib().mpaso_state_launch_config(self._h, c))
         return self._cfg_dict(c)
 
-    def set_launch_config(self, unroll, threads):
-        c = (ctypes.c_int32 * 6)(*[int(x) for x in list(unroll) + list(threads)])
+    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0):
+        c = (ctypes.c_int32 * 10)(*[int(x) for x in list(unroll) + list(threads) + list(capped) + [l2]])
         check(lib().mpaso_state_set_launch_config(self._h, c))
 
     def autotune(self, dt, nsteps=3):
         """Times every launch variant of each stage kernel on this mesh and keeps
         the fastest; (h, u, tracers) are restored afterwards.  Returns the choice."""
-        c = (ctypes.c_int32 * 6)()
+        c = (ctypes.c_int32 * 10)()
         check(lib().mpaso_state_autotune(self._h, ctypes.c_double(dt), int(nsteps), c))
         return self._cfg_dict(c)
 

@@ -46,7 +46,9 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
         b1 += 8 * cl * T + 8 * nE
         f1 += el
         if fct:
-            b1 += 20 * Na * nE + 4 * el + 16 * el * T  # advCells + {cp, cm} pairs, hoMask, LO, A
+            # advCells + the one coefficient the flux sign selects (the {cp, cm} pair the kernel
+            # loads is 8 B more per slot), hoMask, LO, A
+            b1 += 12 * Na * nE + 4 * el + 16 * el * T
             f1 += el * T * (Na + 3)
         else:
             b1 += 8 * el * T
@@ -55,12 +57,13 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b1 += 8 * nE + 8 * el * T
             f1 += el * (1 + 2 * T)
     # ---- K2 edges + cells
-    b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * nE + 8 * cl + 8 * nE
+    # TRiSK stencil (eoe, W/8), F and F Pv gathers, Pv, invDc, bern, coe; u update
+    b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * nE
     b2 += 8 * el + 16 * el + 8 * el * 0.75
-    f2 = el * (2 * Ne + 6 + 1.75)
+    f2 = el * (2 * Ne + 3 + 1.75)  # 2 per slot, q, bern difference, gradient FMA, update
     if visc:
-        b2 += 8 * cl + 8 * vl + 24 * nE
-        f2 += 4 * el
+        b2 += 8 * vl + 16 * nE  # vorticity gather, nu / dv, voe
+        f2 += 2 * el
     b2 += 4 * nC + 12 * slot_c + 8 * nC + 8 * cl + 16 * cl + 8 * cl * 0.75
     f2 += cl * (Nc + 1.75)
     if T:
@@ -68,26 +71,26 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
         if fct:
             b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
             # 1/hProv (6), dt/area, dt/(area hProv); per tracer 3 sums per edge, trUp (3),
-            # numerators / denominators (4), two guarded rcp_nr quotients (12)
+            # numerators / denominators (4), two guarded quotients (12)
             f2 += cl * (8 + T * (3 * Nc + 19))
         else:
             b2 += 8 * el * T + 8 * cl * T
             f2 += cl * T * Nc
     # ---- K3 cells + vertices
-    b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl  # diag: kw, u_next, invArea, ke
-    f3 = cl * (2 * Nc + 1)
+    b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl + 8 * cl + 8 * nC  # kw, u_next, invArea, h_next, bern, g b
+    f3 = cl * (2 * Nc + 2)
     if visc:
-        b3 += 8 * slot_c + 8 * cl
-        f3 += cl * (Nc + 1)
+        b3 += 8 * slot_c + 8 * nC  # sdv, nu / area
+        f3 += cl * Nc
     if T:
-        b3 += 4 * nC + 12 * slot_c + 8 * nE + 8 * cl * 2 + 8 * cl * T * 2 + 16 * cl * T + 8 * cl * T * 0.75
+        b3 += 4 * nC + 12 * slot_c + 8 * nE + 8 * cl + 8 * cl * T * 2 + 16 * cl * T + 8 * cl * T * 0.75
         if fct:
             b3 += 8 * el * T + 16 * cl * T
         if hmix:
             b3 += 8 * el * T
         f3 += cl * (5 + T * (Nc * (1 + int(fct) + int(hmix)) + 4.75))
     b3 += 8 * nV * (3 + 1.5 + 3 + 1.5 + 3) + 8 * vl + 16 * vl
-    f3 += vl * 14
+    f3 += vl * 14  # circulation and kite sums (6), vorticity, f A + circ, 1/hs (5), pv
     return {"sw_edge_pre": (b1, f1), "sw_tend": (b2, f2), "sw_final": (b3, f3)}
 
 
@@ -100,7 +103,7 @@ def ocean_kernels(d: Dims, fct=True, hmix=True):
     b1 = 8 * nE + 8 * el + 8 * cl * T + 8 * nE + 8 * el  # coe, F, tr_in, dv, hE
     f1 = el
     if fct:
-        b1 += 20 * Na * nE + 4 * el + 16 * el * T
+        b1 += 12 * Na * nE + 4 * el + 16 * el * T
         f1 += el * T * (Na + 3)
     if hmix:
         b1 += 8 * nE + 8 * el * T

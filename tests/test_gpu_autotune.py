@@ -15,8 +15,8 @@ from test_gpu_rk4 import make_state
 pytestmark = pytest.mark.gpu
 TOL1 = 1e-12
 
-CONFIGS = [([1, 1, 1], [256, 256, 256]), ([0, 0, 0], [256, 256, 256]), ([1, 1, 1], [64, 128, 64]),
-           ([0, 1, 0], [128, 64, 256])]
+CONFIGS = [([1, 1, 1], [256, 256, 256], [0, 0, 0], 0), ([0, 0, 0], [256, 256, 256], [1, 1, 1], 1),
+           ([1, 1, 1], [64, 128, 64], [1, 0, 1], 2), ([0, 1, 0], [128, 64, 256], [0, 1, 0], 1)]
 
 
 def _fields(st, app):
@@ -33,7 +33,10 @@ def test_every_launch_variant_matches_goldens(name, cfg):
     g = Golden(name)
     dm, st = make_state(g)
     st.set_launch_config(*CONFIGS[cfg])
-    assert st.launch_config() == {"unroll": CONFIGS[cfg][0], "threads": CONFIGS[cfg][1]}
+    got_cfg = st.launch_config()
+    assert {k: got_cfg[k] for k in ("unroll", "threads", "capped")} == {
+        "unroll": CONFIGS[cfg][0], "threads": CONFIGS[cfg][1], "capped": CONFIGS[cfg][2]}
+    assert got_cfg["l2"] in (0, CONFIGS[cfg][3])  # 0 where the state has no such array
     st.step_graph(g.dt, 1)
     got = _fields(st, g.app)
     want = [g["tr_1"]] + ([g["h_1"], g["u_1"]] if g.app == "sw" else [])
@@ -66,6 +69,7 @@ def test_autotune_restores_state_and_keeps_parity(name):
     st.step_graph(g.dt, 0)  # captures a step graph with the default launch shapes
     cfg = st.autotune(g.dt, 2)
     assert all(b in (64, 128, 256) for b in cfg["threads"]) and all(u in (0, 1) for u in cfg["unroll"])
+    assert all(o in (0, 1) for o in cfg["capped"]) and cfg["l2"] in (0, 1, 2)
     assert st.launch_config() == cfg
     for a, b in zip(_fields(st, g.app), before):
         assert np.array_equal(a, b)
@@ -86,6 +90,10 @@ def test_bad_launch_config_is_rejected():
     assert e.value.code == 1
     with pytest.raises(mpaso.MpasoError):
         st.set_launch_config([2, 1, 1], [256, 256, 256])
+    with pytest.raises(mpaso.MpasoError):
+        st.set_launch_config([1, 1, 1], [256, 256, 256], [0, 3, 0])
+    with pytest.raises(mpaso.MpasoError):
+        st.set_launch_config([1, 1, 1], [256, 256, 256], [0, 0, 0], 5)
     assert st.launch_config()["threads"] == [256, 256, 256]
     st.close()
     dm.close()
