@@ -81,8 +81,39 @@ def build_ref(force=False):
         _run(["g++", "-shared", "-o", out, *objs, "-lm"])
         return cfg, out
 
-    with ThreadPoolExecutor(max_workers=len(REF_CONFIGS)) as ex:
-        return dict(ex.map(one, REF_CONFIGS))
+    with ThreadPoolExecutor(max_workers=len(REF_CONFIGS) + 1) as ex:
+        cstep = ex.submit(build_cstep, force)
+        out = dict(ex.map(one, REF_CONFIGS))
+        out["cstep"] = cstep.result()
+        return out
+
+
+CSTEP_LEVELS = 2  # levels of the complex-step build of the sw tasks
+
+
+def build_cstep(force=False):
+    """oracle/_ref/libref_cstep_L<L>.so: apps/sw/tasks/solve.cc with complex state
+    fields (shim MPASO_REF_COMPLEX_STEP) + ref_cstep.cc; None without a checkout."""
+    if not ref_available():
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    shim = os.path.join(HERE, "shim")
+    deps = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs]
+    deps += [os.path.join(HERE, f) for f in ("ref_cstep.cc", "oracle.h", "build.py")]
+    out = os.path.join(out_dir, f"libref_cstep_L{CSTEP_LEVELS}.so")
+    if not (force or _stale(out, deps)):
+        return out
+    defs = [f"-DMPASO_REF_NVL={CSTEP_LEVELS}", "-DMPASO_REF_NTR=1", f"-DMPASO_REF_GRAVITY={GRAVITY}",
+            "-DMPASO_REF_COMPLEX_STEP"]
+    objs = []
+    for path in (os.path.join(REF, "apps/sw/tasks/solve.cc"), os.path.join(HERE, "ref_cstep.cc")):
+        obj = os.path.join(out_dir, "cstep_" + os.path.basename(path) + ".o")
+        _run(["g++", "-std=c++17", *CFLAGS, *defs, f"-I{shim}", f"-I{REF}", f"-I{HERE}", "-w", "-c", path,
+              "-o", obj])
+        objs.append(obj)
+    _run(["g++", "-shared", "-o", out, *objs, "-lm"])
+    return out
 
 
 if __name__ == "__main__":

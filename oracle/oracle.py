@@ -195,3 +195,37 @@ class Oracle:
             else:
                 conv.append(a)
         self._check(getattr(self.lib, "orc_" + name)(*conv))
+
+
+def cstep_path():
+    return os.path.join(HERE, "_ref", "libref_cstep_L2.so")
+
+
+def cstep_available():
+    return os.path.exists(cstep_path())
+
+
+class RefComplexStep:
+    """Complex-step tangent of the reference's own sw RK4 step (ref_cstep.cc):
+    the reference tasks evaluated on complex state, nu = 0, wind not pinned,
+    passive zero tracers, levels fixed by the build (2)."""
+
+    def __init__(self):
+        if not cstep_available():
+            raise FileNotFoundError(f"{cstep_path()} not built (python oracle/build.py)")
+        self.lib = ctypes.CDLL(cstep_path())
+        self.lib.orc_cstep_last_error.restype = ctypes.c_char_p
+        L = ctypes.c_int32()
+        self.lib.orc_cstep_levels(ctypes.byref(L))
+        self.L = L.value
+        self._o = Oracle("restatement")  # for the mesh / static argument structs
+
+    def jvp(self, mesh, dt, nsteps, h, u, dh, du, eps=1e-30):
+        """((h_N, u_N), (dh_N, du_N)) of nsteps steps from (h, u) along (dh, du)."""
+        arrs = [np.ascontiguousarray(a, np.float64).copy() for a in (h, u, dh, du)]
+        om, st = self._o.mesh(mesh), Oracle.static(mesh)
+        rc = self.lib.orc_cstep_sw_run(ctypes.byref(om), ctypes.byref(st), ctypes.c_double(dt),
+                                       ctypes.c_int32(nsteps), ctypes.c_double(eps), *[_ptr(a) for a in arrs])
+        if rc != 0:
+            raise RuntimeError("oracle: " + self.lib.orc_cstep_last_error().decode())
+        return (arrs[0], arrs[1]), (arrs[2], arrs[3])

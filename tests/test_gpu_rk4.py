@@ -108,3 +108,58 @@ def test_host_boundary_call_matches():
     h, u, tr = g["h0"].copy(), g["u0"].copy(), g["tr0"].copy()
     st.step_host(g.dt, 1, h, u, tr)
     assert rel_max(h, g["h_1"]) < TOL1 and rel_max(u, g["u_1"]) < TOL1 and rel_max(tr, g["tr_1"]) < TOL1
+
+
+def _run_both(mesh, fct, state, L, T, dt, n, **opts):
+    """(gpu fields, oracle fields) after n steps from `state` = (h, u, tr)."""
+    import mpaso.gpu as G
+    S = Oracle("restatement")
+    want = S.sw_run(mesh, S.static(mesh, fct), S.config(L, T, **opts), dt, n, *state)
+    dm = G.DeviceMesh(mesh, fct=fct)
+    st = G.State(dm, nlev=L, ntr=T, **opts)
+    st.set(G.FIELD_H, state[0])
+    st.set(G.FIELD_U, state[1])
+    if T:
+        st.set(G.FIELD_TRACERS, state[2])
+    st.step_graph(dt, n)
+    got = (st.get(G.FIELD_H), st.get(G.FIELD_U), st.get(G.FIELD_TRACERS) if T else state[2])
+    st.close()
+    dm.close()
+    return got, want
+
+
+def test_planar_64x64_plain_method_100_steps():
+    """The reference's CPU-runnable configuration: 64 x 64 doubly periodic hex
+    mesh (dc = 10 km, f = 1e-4, g = 9.81, H0 = 1000 m, bumps of 10 m, peak u 1 m/s),
+    FP64 shallow water with del2 viscosity 1e3, dt = 30 s: 1e-12 after one step and
+    1e-9 after 100 against the oracle."""
+    mesh = mpaso.Mesh.hex(64, 64, 10e3, 1e-4)
+    h, u, _ = sw_state(mesh, 7, 1, 0)
+    state = (h, u, np.zeros((mesh.nCells, 1, 0)))
+    opts = dict(gravity=9.81, nu=1e3)
+    for n, tol in ((1, TOL1), (100, TOL100)):
+        got, want = _run_both(mesh, None, state, 1, 0, 30.0, n, **opts)
+        assert rel_max(got[0], want[0]) < tol and rel_max(got[1], want[1]) < tol, n
+
+
+def test_sw_case1_on_device():
+    """Williamson case 1 through the CUDA path: the reference's 0.0015 bound after its
+    ctest (5 steps of 40 s on a 240 km sphere), matching the oracle's h."""
+    from mpaso.testcases import sw_case1, sw_case1_error
+    mesh = mpaso.Mesh.icosa(5)
+    h, u = sw_case1(mesh)
+    got, want = _run_both(mesh, None, (h, u, np.zeros((mesh.nCells, 1, 0))), 1, 0, 40.0, 5, pin_u=True)
+    assert np.array_equal(got[1], u)
+    assert rel_max(got[0], want[0]) < TOL1 * 10 * 5
+    assert sw_case1_error(mesh, got[0], 200.0) <= 0.0015
+
+
+def test_del2_mode_decay_on_device():
+    from mpaso.testcases import del2_mode
+    mesh = mpaso.Mesh.hex(32, 32, 10e3, 0.0)
+    h, u, pattern, k2 = del2_mode(mesh)
+    nu, dt, n = 1e5, 30.0, 100
+    got, want = _run_both(mesh, None, (h, u, np.zeros((mesh.nCells, 1, 0))), 1, 0, dt, n, nu=nu)
+    a = float((got[1][:, 0] * pattern).sum() / (pattern * pattern).sum()) / 1e-6
+    assert abs(-np.log(a) / (nu * dt * n) / k2 - 1) < 0.01
+    assert rel_max(got[1], want[1]) < TOL100

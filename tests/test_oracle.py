@@ -93,3 +93,29 @@ def test_complex_step_restatement(kind, nu):
     fh, fu = (hp - hm) / (2 * eps), (up - um) / (2 * eps)
     assert np.abs(jh.ravel() - fh.ravel()).max() <= 1e-8 * np.abs(fh).max()
     assert np.abs(ju.ravel() - fu.ravel()).max() <= 1e-8 * np.abs(fu).max()
+
+
+@pytest.mark.skipif(not __import__("oracle").cstep_available(), reason="reference checkout absent")
+@pytest.mark.parametrize("kind", ["icosa3", "hex"])
+def test_complex_step_restatement_pinned_to_reference_code(kind):
+    """The reference's own sw tasks evaluated on complex state (shim complex-step
+    build, an FP64 tape over the reference step) give the same real step as the
+    restatement, bit for bit, and the same tangent as the array restatement that
+    the GPU adjoint test uses, to rounding."""
+    import mpaso
+    from mpaso.initial import sw_state
+    from oracle import RefComplexStep
+    from sw_complex import SwComplex
+    mesh = mpaso.Mesh.icosa(3) if kind == "icosa3" else mpaso.Mesh.hex(12, 10, 20e3)
+    dt = 300.0 if kind == "icosa3" else 30.0
+    R = RefComplexStep()
+    h, u, _ = sw_state(mesh, 5, R.L, 1)
+    rng = np.random.default_rng(1)
+    dh, du = rng.standard_normal(h.shape), rng.standard_normal(u.shape) * 1e-3
+    (hr, ur), (jh, ju) = R.jvp(mesh, dt, 4, h, u, dh, du)
+    S = Oracle("restatement")
+    h2, u2, _ = S.sw_run(mesh, S.static(mesh), S.config(R.L, 1), dt, 4, h, u, np.zeros((mesh.nCells, R.L, 1)))
+    assert np.array_equal(hr, h2) and np.array_equal(ur, u2)
+    ch, cu = SwComplex(mesh, R.L).jvp(h, u, dh, du, dt, 4)
+    assert np.abs(jh.ravel() - ch.ravel()).max() <= 1e-14 * np.abs(ch).max()
+    assert np.abs(ju.ravel() - cu.ravel()).max() <= 1e-14 * np.abs(cu).max()
