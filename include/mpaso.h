@@ -239,8 +239,8 @@ int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
  * config[0..2] = 1 where the kernel's stencil loop is unrolled at compile
  * time (only meaningful where the mesh's widest stencil is 10: the sphere),
  * config[3..5] = threads per block (64, 128 or 256), config[6..8] = 1 where
- * the kernel runs with registers capped at 32 per thread for full occupancy
- * (sw app with at most 2 tracers; otherwise ignored), config[9] = static
+ * the kernel runs with registers capped at 40 per thread (1536 threads per
+ * SM; sw app with at most 1 tracer; otherwise ignored), config[9] = static
  * array kept resident in the L2 cache's persisting portion (sw app): 0 none,
  * 1 the FCT advection coefficients, 2 the TRiSK weights.  Results do not
  * depend on the threads per block or the L2 choice; the other variants may

@@ -42,6 +42,9 @@ struct DMesh {
   const int *eocAsc;          // [maxEoC][nC] edges of c by ascending reference edge id
   const double *eocAscSign;   // [maxEoC][nC] sign for eocAsc (-1: c is cells(e)[0])
   const int *coc;             // [maxEoC][nC] cellsOnCell, file order
+  // [maxEoC][nC] the cell across eoc[j][c], shifted left one bit, | 1 where c
+  // is cells(e)[0] of that edge (pads: own index, bit 0)
+  const int *nbr;
   const double *areaCell, *invAreaCell, *bottomDepth;
   const int *maxLevelCell;    // [nC]
   // ---- edges ----

@@ -191,6 +191,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   DMesh &m = ctx.d;
   m.nC = (int)nC, m.nE = (int)nE, m.nV = (int)nV, m.maxEoC = maxEoC, m.maxEoE = maxEoE;
   std::vector<int> nEoC(nC), eoc((size_t)maxEoC * nC), eocAsc((size_t)maxEoC * nC), coc((size_t)maxEoC * nC);
+  std::vector<int> nbr((size_t)maxEoC * nC);
   std::vector<double> eocSign((size_t)maxEoC * nC, 0.0), eocAscSign((size_t)maxEoC * nC, 0.0);
   std::vector<double> area(nC), invArea(nC), hs(nC, 0.0);
   std::vector<int> mlc(nC, 1);
@@ -205,6 +206,8 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
         const int32_t e = c2e.at(c, j);
         eoc[s] = ie[e];
         coc[s] = ic[c2c.at(c, j)];
+        const bool first = c == e2c.at(e, 0);
+        nbr[s] = (int)(((uint32_t)ic[first ? e2c.at(e, 1) : e2c.at(e, 0)] << 1) | (first ? 1u : 0u));
         eocSign[s] = d.edgeSignOnCell ? d.edgeSignOnCell[(size_t)c * kMaxEdges + j]
                                       : (c == e2c.at(e, 0) ? -1.0 : 1.0);
         const int32_t ea = c2eAsc.at(c, j);
@@ -213,6 +216,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
       } else {  // pad: repeat slot 0 with a zero sign
         eoc[s] = ie[c2e.at(c, 0)];
         coc[s] = k;
+        nbr[s] = (int)((uint32_t)k << 1);
         eocAsc[s] = ie[c2e.at(c, 0)];
       }
     }
@@ -222,7 +226,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     if (d.maxLevelCell) mlc[k] = d.maxLevelCell[c];
   }
   A.add(nEoC, &m.nEoC), A.add(eoc, &m.eoc), A.add(eocSign, &m.eocSign), A.add(eocAsc, &m.eocAsc);
-  A.add(eocAscSign, &m.eocAscSign), A.add(coc, &m.coc), A.add(area, &m.areaCell);
+  A.add(eocAscSign, &m.eocAscSign), A.add(coc, &m.coc), A.add(nbr, &m.nbr), A.add(area, &m.areaCell);
   A.add(invArea, &m.invAreaCell), A.add(hs, &m.bottomDepth), A.add(mlc, &m.maxLevelCell);
 
   // ---- edges ----

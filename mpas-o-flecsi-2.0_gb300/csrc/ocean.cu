@@ -46,21 +46,22 @@ __global__ void __launch_bounds__(TPB) k_oc_edges(DMesh m, DStat st, Stage S, in
                             m.dvEdge, st.cpm1, st.kd);
 }
 
-template <int T>
+// NC = 6: cell loops unrolled over 6 slots (meshes with at most 6 edges per cell)
+template <int T, int NC>
 __global__ void __launch_bounds__(TPB) k_oc_cells(DMesh m, Stage S, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nC * L) return;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-  cell_limiter<T>(m, S, L, c, k, i, S.h_in[i], S.hpi[i]);
+  cell_limiter<T, NC>(m, S, L, c, k, i, S.h_in[i], S.hpi[i]);
 }
 
-template <int T>
+template <int T, int NC>
 __global__ void __launch_bounds__(TPB) k_oc_final(DMesh m, Stage S, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nC * L) return;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   double tend[T];
-  cell_tracer_tend<T>(m, S, L, c, k, i, tend);
+  cell_tracer_tend<T, NC>(m, S, L, c, k, i, tend);
 #pragma unroll
   for (int t = 0; t < T; ++t) {
     const int64_t j = i * T + t;
@@ -91,7 +92,7 @@ Stage ocean_stage(SwState &s, int rk, double dt) {
   S.tr_out = rk < 3 ? trs[rk + 1] : nullptr;
   S.tr_prev = s.TR0, S.trh_acc = s.TRH, S.tr_new = s.TR0;
   S.h_in = s.H[0], S.u_in = s.U[0];
-  S.F = s.F, S.A = s.A, S.LO = s.LO, S.DF = s.DF, S.Rp = s.Rp, S.Rm = s.Rm, S.tLO = s.tLO;
+  S.F = s.F, S.A = s.A, S.LO = s.LO, S.DF = s.DF, S.R2 = s.R2, S.tLO = s.tLO;
   S.hE = s.HE, S.hpi = s.HPI;
   return S;
 }
@@ -106,9 +107,16 @@ template <int T> void ocean_stage_T(SwState &s, const Stage &S, cudaStream_t st)
   else
     k_oc_edges<T, 0><<<blocks_for((int64_t)m.nE * L, b0), b0, 0, st>>>(m, s.st, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
-  k_oc_cells<T><<<blocks_for((int64_t)m.nC * L, b1), b1, 0, st>>>(m, S, L);
+  const bool c6 = m.maxEoC <= 6;
+  if (c6 && s.tune_unroll[1])
+    k_oc_cells<T, 6><<<blocks_for((int64_t)m.nC * L, b1), b1, 0, st>>>(m, S, L);
+  else
+    k_oc_cells<T, 0><<<blocks_for((int64_t)m.nC * L, b1), b1, 0, st>>>(m, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
-  k_oc_final<T><<<blocks_for((int64_t)m.nC * L, b2), b2, 0, st>>>(m, S, L);
+  if (c6 && s.tune_unroll[2])
+    k_oc_final<T, 6><<<blocks_for((int64_t)m.nC * L, b2), b2, 0, st>>>(m, S, L);
+  else
+    k_oc_final<T, 0><<<blocks_for((int64_t)m.nC * L, b2), b2, 0, st>>>(m, S, L);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
@@ -121,7 +129,7 @@ void ocean_create(SwState &s) {
       {&s.U[0], nE * L}, {&s.H[0], nC * L}, {&s.HE, nE * L}, {&s.HPI, nC * L},
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
       {&s.F, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T}, {&s.DF, nE * L * T},
-      {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T}};
+      {(double **)&s.R2, 2 * nC * L * T}, {&s.tLO, nC * L * T}};
   stat_buffers(s, bufs);
   alloc_arena(s, bufs);
   build_stat(s);

@@ -33,10 +33,10 @@ constexpr int TPB = 256;
 // Launch-shape variants of the stage kernels (picked per mesh by the autotuner):
 // NW = 10: edgesOnEdge and advection stencils of exactly 10 slots (hexagon /
 // pentagon meshes), unrolled at compile time; NW = 0: runtime widths.
-// OC = 1: registers capped at 32 so 2048 threads fit an SM (more warps to hide
+// OC = 1: registers capped at 40 so 1536 threads fit an SM (more warps to hide
 // gather latency, less ILP per warp); OC = 0: the compiler's choice.
-constexpr int kOccMaxT = 2;  // OC = 1 variants exist up to this many tracers
-#define MPASO_BOUNDS(OC) __launch_bounds__(TPB, (OC) ? 2048 / TPB : 1)
+constexpr int kOccMaxT = 1;  // OC = 1 variants exist up to this many tracers (beyond, they spill)
+#define MPASO_BOUNDS(OC) __launch_bounds__(TPB, (OC) ? 1536 / TPB : 0)
 
 // ------------------------------------------------------------- K1: edges
 template <int T, int NW, int OC>
@@ -50,8 +50,7 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
   const double hs = S.h_in[i1] + S.h_in[i2];  // 2 h_edge
   const double F = S.u_in[i] * hs;            // 2 u h_edge
   const double pv2 = S.pv[(int64_t)v.x * L + k] + S.pv[(int64_t)v.y * L + k];  // 2 pv_edge
-  S.F[i] = F;
-  S.G[i] = F * pv2;
+  S.FG[i] = make_double2(F, F * pv2);
   S.pve[i] = pv2;
   if constexpr (T > 0) edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, F, hs, st.dvh, st.cpm2, st.kdh);
 }
@@ -71,15 +70,18 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
       const int eo = m.eoe[(int64_t)j * m.nE + e];
       const double w = st.woe8[(int64_t)j * m.nE + e];
       const int64_t io = (int64_t)eo * L + k;
-      s1 = fma(w, S.F[io], s1);
-      s2 = fma(w, S.G[io], s2);
+      const double2 fg = S.FG[io];
+      s1 = fma(w, fg.x, s1);
+      s2 = fma(w, fg.y, s2);
     }
     const double q = fma(S.pve[i], s1, s2);
     const int2 c = m.coe[e];
     const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-    // - (ke2 - ke1 + g (h2 + b2 - h1 - b1)) / dc + nu (div2 - div1) / dc as one
-    // gradient of the cell function bern = ke + g (h + b) - nu div
-    double tend = fma(-m.invDcEdge[e], S.bern[i2] - S.bern[i1], q);
+    // - (ke2 - ke1 + g (h2 + b2 - h1 - b1)) / dc + nu (div2 - div1) / dc, with the
+    // kinetic and divergence parts as one difference of kdiv = ke - nu div; the
+    // geopotential stays a thickness difference, exact where h is uniform
+    const double dh = (S.h_in[i2] - S.h_in[i1]) + st.dhs[e];
+    double tend = fma(-m.invDcEdge[e], fma(S.g, dh, S.bern[i2] - S.bern[i1]), q);
     if (S.visc) {  // - nu (vort_b - vort_a) / dv
       const int2 v = m.voe[e];
       tend = fma(-st.nuDv[e], S.vort[(int64_t)v.y * L + k] - S.vort[(int64_t)v.x * L + k], tend);
@@ -101,13 +103,14 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   }
   i -= nEL;
   if (i >= (int64_t)m.nC * L) return;
+  constexpr int NC = NW > 0 ? 6 : 0;  // the unrolled variant also unrolls the cell loops
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c];
-  double tend_h = 0.0;  // sum edgeSign dv F / area, from F2 with the halved weights
-  for (int j = 0; j < n; ++j) {
-    const int e = m.eoc[(int64_t)j * m.nC + c];
-    tend_h = fma(st.sdvi[(int64_t)j * m.nC + c], S.F[(int64_t)e * L + k], tend_h);
-  }
+  double tend_h = 0.0;  // sum edgeSign dv F / area, from F2 with the halved weights (0 in pads)
+  for_slots<NC>(n, [&](int j, bool) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    tend_h = fma(st.sdvi[s], S.FG[(int64_t)m.eoc[s] * L + k].x, tend_h);
+  });
   const double hp = S.h_prev[i];
   switch (S.stage) {
     case 0:
@@ -125,28 +128,47 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
     // provisional thickness (apps/ocean/tasks/solve.cc:60-97): h + dt tend_h
     const double hin = S.h_in[i];
     const double hpi = S.fct ? rcp_nr(fma(S.dt, tend_h, hin)) : 0.0;
-    cell_limiter<T>(m, S, L, c, k, i, hin, hpi);
+    cell_limiter<T, NC>(m, S, L, c, k, i, hin, hpi);
   }
 }
 
-// Diagnostics of a state (u, h): at cells the Bernoulli-type function
-// bern = ke + g (h + b) - nu div whose edge difference / dcEdge is the whole
-// gradient part of tend_u (apps/sw/tasks/solve.cc:228-231 plus del2
-// momentum); vorticity and pv at vertices.
-__device__ __forceinline__ void cell_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
-                                          int c, int k, int64_t i, const double *u, double h) {
-  const int n = m.nEoC[c];
+// Diagnostics of a state (u, h): at cells kdiv = ke - nu div, whose edge
+// difference / dcEdge is the kinetic-energy gradient of tend_u
+// (apps/sw/tasks/solve.cc:228-231) plus the divergence part of del2
+// momentum; vorticity and pv at vertices.  CellDiag accumulates the edge sums
+// of one cell (ke, the divergence numerator) slot by slot.  (Folding g (h + b)
+// into the same cell function would save two more instructions per edge but
+// leaves an absolute error floor of ulp(g h) / dcEdge in tend_u, which breaks
+// the relative parity bar for slow flows.)
+struct CellDiag {
+  const DStat &st;
+  const Stage &S;
+  const double *u;
+  int L, k;
   double ke = 0.0, dv = 0.0;
-  for (int j = 0; j < n; ++j) {
-    const int e = m.eoc[(int64_t)j * m.nC + c];
+  __device__ void operator()(int64_t s, int e, bool valid) {
     const double ue = u[(int64_t)e * L + k];
-    ke = fma(st.kw[e], ue * ue, ke);
-    if (S.visc) dv = fma(st.sdv[(int64_t)j * m.nC + c], ue, dv);
+    const double kn = fma(st.kw[e], ue * ue, ke);
+    ke = valid ? kn : ke;
+    if (S.visc) dv = fma(st.sdv[s], ue, dv);  // sdv is 0 in pad slots
   }
-  double b = fma(S.g, h, fma(ke, m.invAreaCell[c], st.gbd[c]));
-  // sdv = edgeSignOnCell dv is inward-positive: div = -dv / area, -nu div = nu dv / area
-  if (S.visc) b = fma(st.nuInva[c], dv, b);
-  S.bern[i] = b;
+  __device__ void finish(const DMesh &m, int c, int64_t i) const {
+    double b = ke * m.invAreaCell[c];
+    // sdv = edgeSignOnCell dv is inward-positive: div = -dv / area, -nu div = nu dv / area
+    if (S.visc) b = fma(st.nuInva[c], dv, b);
+    S.bern[i] = b;
+  }
+};
+
+template <int NC>
+__device__ __forceinline__ void cell_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
+                                          int c, int k, int64_t i, const double *u) {
+  CellDiag d{st, S, u, L, k};
+  for_slots<NC>(m.nEoC[c], [&](int j, bool ok) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    d(s, m.eoc[s], ok);
+  });
+  d.finish(m, c, i);
 }
 
 __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, const Stage &S, int L,
@@ -165,7 +187,7 @@ __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, con
 }
 
 // ------------------------------------------------------ K3: cells + vertices
-template <int T, int OC>
+template <int T, int NC, int OC>
 __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
@@ -173,10 +195,13 @@ __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
   const double *h_next = S.stage == 3 ? S.h_new : S.h_out;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    const double hn = h_next[i];
     if constexpr (T > 0) {
+      const double hn = h_next[i];
+      // one pass over the cell's edges: tracer tendency and the next state's diagnostics
+      CellDiag d{st, S, u_next, L, k};
       double tend[T];
-      cell_tracer_tend<T>(m, S, L, c, k, i, tend);
+      cell_tracer_tend<T, NC>(m, S, L, c, k, i, tend, d);
+      d.finish(m, c, i);
       const double rh = rcp_nr(hn);
       const double hpv = S.h_prev[i];
 #pragma unroll
@@ -196,8 +221,9 @@ __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
             S.trh_acc[i * T + t] = fma(S.w_acc, tend[t], S.trh_acc[i * T + t]);
         }
       }
+    } else {
+      cell_diag<NC>(m, st, S, L, c, k, i, u_next);
     }
-    cell_diag(m, st, S, L, c, k, i, u_next, hn);
     return;
   }
   i -= nCL;
@@ -212,7 +238,7 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    cell_diag(m, st, S, L, c, k, i, S.u_in, S.h_in[i]);
+    cell_diag<0>(m, st, S, L, c, k, i, S.u_in);
     return;
   }
   i -= nCL;
@@ -223,12 +249,12 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
 
 // Derived statics of a state.
 struct StatOut {
-  double *sdv, *sdvi, *kw, *sdc, *gbd, *kd, *kdh, *dvh, *woe8;
+  double *sdv, *sdvi, *kw, *sdc, *dhs, *kd, *kdh, *dvh, *woe8;
   double2 *cpm2, *cpm1;
   double *nuInva, *nuDv;
 };
 
-__global__ void k_build_stat(DMesh m, double g, double kappa, double nu, StatOut o) {
+__global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < (int64_t)m.maxEoC * m.nC) {
     const int c = (int)(i % m.nC), j = (int)(i / m.nC);
@@ -236,12 +262,11 @@ __global__ void k_build_stat(DMesh m, double g, double kappa, double nu, StatOut
     o.sdv[i] = s;
     o.sdvi[i] = 0.5 * s * m.invAreaCell[c];
   }
-  if (i < m.nC) {
-    o.gbd[i] = g * m.bottomDepth[i];
-    o.nuInva[i] = nu * m.invAreaCell[i];
-  }
+  if (i < m.nC) o.nuInva[i] = nu * m.invAreaCell[i];
   if (i < m.nE) {
     o.kw[i] = 0.25 * m.dcEdge[i] * m.dvEdge[i];
+    const int2 c = m.coe[i];
+    o.dhs[i] = m.bottomDepth[c.y] - m.bottomDepth[c.x];
     const double kd = m.meshScalingDel2[i] * kappa * m.dvEdge[i] * m.invDcEdge[i];
     o.kd[i] = kd;
     o.kdh[i] = 0.5 * kd;
@@ -291,10 +316,10 @@ void build_stat(SwState &s) {
   const int64_t nmax2 = std::max<int64_t>(nmax, std::max<int64_t>((int64_t)m.maxEoE * m.nE,
                                                                   (int64_t)m.maxAdv * m.nE));
   StatOut o{(double *)s.st.sdv, (double *)s.st.sdvi, (double *)s.st.kw, (double *)s.st.sdc,
-            (double *)s.st.gbd, (double *)s.st.kd, (double *)s.st.kdh, (double *)s.st.dvh,
+            (double *)s.st.dhs, (double *)s.st.kd, (double *)s.st.kdh, (double *)s.st.dvh,
             (double *)s.st.woe8, (double2 *)s.st.cpm2, (double2 *)s.st.cpm1, (double *)s.st.nuInva,
             (double *)s.st.nuDv};
-  k_build_stat<<<blocks_for(nmax2, TPB), TPB, 0, s.stream>>>(m, s.p.gravity, s.p.kappa, s.p.nu, o);
+  k_build_stat<<<blocks_for(nmax2, TPB), TPB, 0, s.stream>>>(m, s.p.kappa, s.p.nu, o);
   MPASO_CUDA(cudaGetLastError());
 }
 
@@ -305,7 +330,7 @@ void stat_buffers(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs) 
   DStat &t = s.st;
   auto P = [](const double *&p) { return (double **)&p; };
   bufs.insert(bufs.end(), {{P(t.sdv), (int64_t)m.maxEoC * nC}, {P(t.sdvi), (int64_t)m.maxEoC * nC},
-                           {P(t.kw), nE}, {P(t.sdc), 3 * nV}, {P(t.gbd), nC}, {P(t.kd), nE},
+                           {P(t.kw), nE}, {P(t.sdc), 3 * nV}, {P(t.dhs), nE}, {P(t.kd), nE},
                            {P(t.kdh), nE}, {P(t.dvh), nE}, {P(t.woe8), (int64_t)m.maxEoE * nE},
                            {(double **)&t.cpm2, 2LL * m.maxAdv * nE},
                            {(double **)&t.cpm1, 2LL * m.maxAdv * nE}, {P(t.nuInva), nC}, {P(t.nuDv), nE}});
@@ -331,8 +356,8 @@ Stage make_stage(SwState &s, int rk, double dt) {
   S.u_acc = s.U[2], S.h_acc = s.H[2], S.trh_acc = s.TRH;
   S.u_new = s.U[0], S.h_new = s.H[0], S.tr_new = s.TR0;
   S.pv = s.pv, S.vort = s.vort, S.bern = s.bern;
-  S.F = s.F, S.G = s.G, S.pve = s.pve, S.A = s.A, S.LO = s.LO, S.DF = s.DF;
-  S.Rp = s.Rp, S.Rm = s.Rm, S.tLO = s.tLO;
+  S.FG = s.FG, S.pve = s.pve, S.A = s.A, S.LO = s.LO, S.DF = s.DF;
+  S.R2 = s.R2, S.tLO = s.tLO;
   return S;
 }
 
@@ -378,15 +403,20 @@ void launch_k2(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_
 }
 
 template <int T, int OC>
-void launch_k3(const SwState &s, const Stage &S, int b, cudaStream_t st) {
+void launch_k3(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
-  k_sw_final<T, OC><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, b), b, 0, st>>>(m, s.st, S, s.L);
+  const int64_t n = ((int64_t)m.nC + m.nV) * s.L;
+  if (unroll)
+    k_sw_final<T, 6, OC><<<blocks_for(n, b), b, 0, st>>>(m, s.st, S, s.L);
+  else
+    k_sw_final<T, 0, OC><<<blocks_for(n, b), b, 0, st>>>(m, s.st, S, s.L);
 }
 
 template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   cudaEvent_t *ev = s.prof_events;
-  const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0);
+  // 10-slot edge stencils (K1, K2 edges) and at most 6 edges per cell (K2, K3 cells)
+  const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0), c6 = m.maxEoC <= 6;
   constexpr int OC1 = T <= kOccMaxT ? 1 : 0;  // no capped variants compiled beyond kOccMaxT
   if (OC1 && s.tune_occ[0])
     launch_k1<T, OC1>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
@@ -394,14 +424,14 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
     launch_k1<T, 0>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
   if (OC1 && s.tune_occ[1])
-    launch_k2<T, OC1>(s, S, w10 && s.tune_unroll[1], s.tune_tpb[1], st);
+    launch_k2<T, OC1>(s, S, w10 && c6 && s.tune_unroll[1], s.tune_tpb[1], st);
   else
-    launch_k2<T, 0>(s, S, w10 && s.tune_unroll[1], s.tune_tpb[1], st);
+    launch_k2<T, 0>(s, S, w10 && c6 && s.tune_unroll[1], s.tune_tpb[1], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
   if (OC1 && s.tune_occ[2])
-    launch_k3<T, OC1>(s, S, s.tune_tpb[2], st);
+    launch_k3<T, OC1>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
   else
-    launch_k3<T, 0>(s, S, s.tune_tpb[2], st);
+    launch_k3<T, 0>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
   if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
 }
 
@@ -454,8 +484,8 @@ void sw_create(SwState &s) {
       {&s.H[0], nC * L}, {&s.H[1], nC * L}, {&s.H[2], nC * L}, {&s.H[3], nC * L},
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
       {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.bern, nC * L},
-      {&s.F, nE * L}, {&s.G, nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
-      {&s.DF, nE * L * T}, {&s.Rp, nC * L * T}, {&s.Rm, nC * L * T}, {&s.tLO, nC * L * T}};
+      {(double **)&s.FG, 2 * nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
+      {&s.DF, nE * L * T}, {(double **)&s.R2, 2 * nC * L * T}, {&s.tLO, nC * L * T}};
   stat_buffers(s, bufs);
   alloc_arena(s, bufs);
   build_stat(s);
@@ -560,8 +590,10 @@ void drop_graph(SwState &S) {
 // Whether kernel k of the stage has a compile-time-unrolled variant on this mesh.
 bool has_unrolled(const SwState &S, int k) {
   const DMesh &m = S.mesh->ctx.d;
-  if (S.p.app == MPASO_APP_OCEAN) return k == 0 && m.maxAdv == 10;
-  return k < 2 && m.maxEoE == 10 && (m.maxAdv == 10 || !S.p.fct || S.T == 0);
+  const bool c6 = m.maxEoC <= 6;
+  if (S.p.app == MPASO_APP_OCEAN) return k == 0 ? m.maxAdv == 10 : c6;
+  const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !S.p.fct || S.T == 0);
+  return k == 0 ? w10 : k == 1 ? w10 && c6 : c6;
 }
 
 // Whether the register-capped (full occupancy) variants exist for this state.

@@ -34,7 +34,7 @@ struct DStat {
   const double *sdvi;  // [maxEoC][nC] 0.5 * edgeSignOnCell * dvEdge / areaCell (tend_h from F2)
   const double *kw;    // [nE] 0.25 * dcEdge * dvEdge
   const double *sdc;   // [3][nV] circulation sign * dcEdge
-  const double *gbd;   // [nC] gravity * bottomDepth
+  const double *dhs;   // [nE] bottomDepth(c2) - bottomDepth(c1)
   const double *kd;    // [nE] meshScalingDel2 * kappa * dvEdge / dcEdge
   const double *kdh;   // [nE] kd / 2 (del2 flux from h1 + h2)
   const double *dvh;   // [nE] dvEdge / 2 (fluxes from F2)
@@ -58,9 +58,12 @@ struct Stage {
   double *u_out, *h_out, *tr_out;           // next stage input (stages 0..2)
   double *u_acc, *h_acc, *trh_acc;          // RK accumulators
   double *u_new, *h_new, *tr_new;           // step result (stage 3)
-  double *pv, *vort, *bern;                 // diagnostics of the stage input
-  double *F, *G, *pve, *A, *LO, *DF;        // edge intermediates
-  double *Rp, *Rm, *tLO;                    // cell intermediates
+  double *pv, *vort, *bern;                 // diagnostics of the stage input (bern: ke - nu div)
+  double *F;                                // ocean: thickness flux u h_e
+  double2 *FG;                              // sw: {F2, F2 Pv} per edge, gathered together
+  double *pve, *A, *LO, *DF;                // edge intermediates
+  double2 *R2;                              // {R+, R-} limiter factors per cell and tracer
+  double *tLO;                              // cell intermediates
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
 };
 
@@ -75,8 +78,9 @@ struct SwState {
   double *U[4]{}, *H[4]{}, *TR0 = nullptr, *TRA = nullptr, *TRB = nullptr, *TRH = nullptr;
   double *HE = nullptr, *HPI = nullptr;
   double *pv = nullptr, *vort = nullptr, *bern = nullptr;
-  double *F = nullptr, *G = nullptr, *pve = nullptr, *A = nullptr, *LO = nullptr, *DF = nullptr;
-  double *Rp = nullptr, *Rm = nullptr, *tLO = nullptr;
+  double *F = nullptr, *pve = nullptr, *A = nullptr, *LO = nullptr, *DF = nullptr;
+  double2 *FG = nullptr, *R2 = nullptr;
+  double *tLO = nullptr;
   DStat st{};
   bool diag_valid = false;  // sw: diagnostics of U[0]/H[0] current
   double prep_dt = 0.0;     // ocean: dt of the cached F / 1/hProv (0 = stale)
@@ -168,87 +172,131 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
   }
 }
 
+// Loop over the edge slots of a cell.  NC > 0 unrolls NC slots at compile
+// time so every slot's loads issue together: pad slots repeat valid indices
+// (own cell, slot-0 edge, zero weights) and `valid` masks what they would
+// add.  NC = 0 loops to the cell's own edge count.  With every real slot
+// valid, both forms add the same terms in the same order.
+template <int NC, class Body>
+__device__ __forceinline__ void for_slots(int n, Body &&body) {
+  if constexpr (NC > 0) {
+#pragma unroll
+    for (int j = 0; j < NC; ++j) body(j, j < n);
+  } else {
+    for (int j = 0; j < n; ++j) body(j, true);
+  }
+}
+
+// v in a real slot, +0 in a pad slot (a select on the integer pipe)
+__device__ __forceinline__ double dmask(double v, bool valid) { return valid ? v : 0.0; }
+
 // Cell bounds, upwind tendency and limiter factors R+ / R- (ocean solve.cc:194-267).
-template <int T>
+template <int T, int NC>
 __device__ __forceinline__ void cell_limiter(const DMesh &m, const Stage &S, int L, int c, int k,
                                              int64_t i, double hin, double hpi) {
   const int n = m.nEoC[c];
-  const double inva = m.invAreaCell[c];
-  if (!S.fct) {
+  double tl[T];
 #pragma unroll
-    for (int t = 0; t < T; ++t) {
-      double tl = 0.0;
-      for (int j = 0; j < n; ++j) {
-        const int e = m.eoc[(int64_t)j * m.nC + c];
-        tl += dflip(S.LO[((int64_t)e * L + k) * T + t], sign_mask(m.eocSign[(int64_t)j * m.nC + c]));
-      }
-      S.tLO[i * T + t] = tl;  // area-weighted; cell_tracer_tend divides by the area
-    }
+  for (int t = 0; t < T; ++t) tl[t] = 0.0;
+  if (!S.fct) {
+    for_slots<NC>(n, [&](int j, bool ok) {
+      const int64_t s = (int64_t)j * m.nC + c;
+      const int64_t ie0 = ((int64_t)m.eoc[s] * L + k) * T;
+      const long long sm = sign_mask(m.eocSign[s]);
+#pragma unroll
+      for (int t = 0; t < T; ++t) tl[t] += dmask(dflip(S.LO[ie0 + t], sm), ok);
+    });
+#pragma unroll
+    for (int t = 0; t < T; ++t) S.tLO[i * T + t] = tl[t];  // area-weighted; divided by the area later
     return;
   }
-  const double dtia = S.dt * inva;  // dt / area
-  const double dthi = dtia * hpi;   // dt / (area hProv)
+  double trc[T], mx[T], mn[T], fi[T], fo[T];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    trc[t] = S.tr_in[i * T + t];
+    mx[t] = trc[t], mn[t] = trc[t], fi[t] = 0.0, fo[t] = 0.0;
+  }
+  for_slots<NC>(n, [&](int j, bool ok) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    const int64_t in0 = ((int64_t)m.coc[s] * L + k) * T;  // pads: the cell itself
+    const int64_t ie0 = ((int64_t)m.eoc[s] * L + k) * T;
+    const long long sm = sign_mask(m.eocSign[s]);
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      const double x = S.tr_in[in0 + t];
+      mx[t] = dmax(mx[t], x);
+      mn[t] = dmin(mn[t], x);
+      tl[t] += dmask(dflip(S.LO[ie0 + t], sm), ok);
+      const double ax = dflip(S.A[ie0 + t], sm);
+      fi[t] += dmask(dpos(ax), ok);
+      fo[t] += dmask(dneg(ax), ok);
+    }
+  });
+  const double dtia = S.dt * m.invAreaCell[c];  // dt / area
+  const double dthi = dtia * hpi;               // dt / (area hProv)
   const double eps = 1.e-10;
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    const double trc = S.tr_in[i * T + t];
-    double mx = trc, mn = trc, tl = 0.0, fi = 0.0, fo = 0.0;
-    for (int j = 0; j < n; ++j) {
-      const int nb = m.coc[(int64_t)j * m.nC + c];
-      const double x = S.tr_in[((int64_t)nb * L + k) * T + t];
-      mx = dmax(mx, x);
-      mn = dmin(mn, x);
-      const int e = m.eoc[(int64_t)j * m.nC + c];
-      const long long sm = sign_mask(m.eocSign[(int64_t)j * m.nC + c]);
-      const int64_t ie = ((int64_t)e * L + k) * T + t;
-      tl += dflip(S.LO[ie], sm);
-      const double ax = dflip(S.A[ie], sm);
-      fi += dpos(ax);
-      fo += dneg(ax);
-    }
     // trUp = (tr h + dt tend) / hProv; trMaxNew - trUp = dt flxIn / hProv, with
     // tend, flxIn, flxOut the area-weighted sums tl, fi, fo divided by the area
-    const double up = fma(dtia, tl, trc * hin) * hpi;
-    const double np = mx - up, dp = fma(dthi, fi, eps);
-    const double nm = up - mn, dm = fma(-dthi, fo, eps);
+    const double up = fma(dtia, tl[t], trc[t] * hin) * hpi;
+    const double np = mx[t] - up, dp = fma(dthi, fi[t], eps);
+    const double nm = up - mn[t], dm = fma(-dthi, fo[t], eps);
     // clamp01(n / d): 0 when n <= 0, 1 when n >= d, the quotient otherwise
     double rp = dgt0(np) ? 1.0 : 0.0, rm = dgt0(nm) ? 1.0 : 0.0;
     if (dgt0(np) && dkey(np) < dkey(dp)) rp = dclamp01(np * rcp_nr(dp));
     if (dgt0(nm) && dkey(nm) < dkey(dm)) rm = dclamp01(nm * rcp_nr(dm));
-    S.Rp[i * T + t] = rp;
-    S.Rm[i * T + t] = rm;
-    S.tLO[i * T + t] = tl;
+    S.R2[i * T + t] = make_double2(rp, rm);
+    S.tLO[i * T + t] = tl[t];
   }
 }
 
 // Tracer tendency of a cell: upwind part + limited anti-diffusive fluxes
-// (ocean solve.cc:269-326) - del2 mixing (solve.cc:340-364).
-template <int T>
-__device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S, int L, int c,
-                                                 int k, int64_t i, double *tend) {
+// (ocean solve.cc:269-326) - del2 mixing (solve.cc:340-364).  One pass over
+// the cell's edges for all tracers; the limiter factors of the cell across
+// each edge come from one 16-byte gather.  With (c1, c2) = cells(e), the
+// reference limits A by min(R-(c1), R+(c2)) for A > 0 and min(R+(c1), R-(c2))
+// otherwise, i.e. by min(R- upstream, R+ downstream).
+struct NoEdgeHook {
+  __device__ void operator()(int64_t, int, bool) const {}
+};
+
+// `hook(slot, edge, valid)` runs once per edge slot of the cell inside the
+// same loop (the sw driver folds the next state's cell diagnostics into it).
+template <int T, int NC, class Hook = NoEdgeHook>
+__device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S, int L, int c, int k,
+                                                 int64_t i, double *tend, Hook &&hook = Hook()) {
   const int n = m.nEoC[c];
-  const double inva = m.invAreaCell[c];
+  double2 own[T];
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    double acc = S.tLO[i * T + t];  // area-weighted upwind part
-    for (int j = 0; j < n; ++j) {
-      const int e = m.eoc[(int64_t)j * m.nC + c];
-      const long long sm = sign_mask(m.eocSign[(int64_t)j * m.nC + c]);
-      const int64_t ie = ((int64_t)e * L + k) * T + t;
+    tend[t] = S.tLO[i * T + t];  // area-weighted upwind part
+    if (S.fct) own[t] = S.R2[i * T + t];
+  }
+  for_slots<NC>(n, [&](int j, bool ok) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    const int e = m.eoc[s];
+    hook(s, e, ok);
+    const long long sm = sign_mask(m.eocSign[s]);
+    const int nb = m.nbr[s];
+    const bool own_first = nb & 1;
+    const int64_t ie0 = ((int64_t)e * L + k) * T, jn = ((int64_t)(nb >> 1) * L + k) * T;
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
       double x = 0.0;
       if (S.fct) {
-        const int2 cc = m.coe[e];
-        const int64_t j1 = ((int64_t)cc.x * L + k) * T + t, j2 = ((int64_t)cc.y * L + k) * T + t;
-        const double a = S.A[ie];
-        // max(0,A) min(R-(c1), R+(c2)) + min(0,A) min(R+(c1), R-(c2))  (solve.cc:276-279)
-        const double r = dgt0(a) ? dmin(S.Rm[j1], S.Rp[j2]) : dmin(S.Rp[j1], S.Rm[j2]);
+        const double a = S.A[ie0 + t];
+        const double2 o = S.R2[jn + t];
+        const double r = dgt0(a) == own_first ? dmin(own[t].y, o.x) : dmin(o.y, own[t].x);
         x = a * r;
       }
-      if (S.hmix) x -= S.DF[ie];
-      acc += dflip(x, sm);
+      if (S.hmix) x -= S.DF[ie0 + t];
+      tend[t] += dmask(dflip(x, sm), ok);
     }
-    tend[t] = acc * inva;
-  }
+  });
+  const double inva = m.invAreaCell[c];
+#pragma unroll
+  for (int t = 0; t < T; ++t) tend[t] *= inva;
 }
 
 }  // namespace mpaso

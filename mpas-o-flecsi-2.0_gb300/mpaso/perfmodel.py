@@ -57,10 +57,10 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b1 += 8 * nE + 8 * el * T
             f1 += el * (1 + 2 * T)
     # ---- K2 edges + cells
-    # TRiSK stencil (eoe, W/8), F and F Pv gathers, Pv, invDc, bern, coe; u update
-    b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * nE
+    # TRiSK stencil (eoe, W/8), {F, F Pv} gathers, Pv, invDc, ke - nu div, h, dhs, coe; u update
+    b2 = 12 * Ne * nE + 16 * el + 8 * el + 8 * nE + 8 * cl + 8 * cl + 8 * nE + 8 * nE
     b2 += 8 * el + 16 * el + 8 * el * 0.75
-    f2 = el * (2 * Ne + 3 + 1.75)  # 2 per slot, q, bern difference, gradient FMA, update
+    f2 = el * (2 * Ne + 6 + 1.75)  # 2 per slot, q, thickness and kdiv differences, 2 FMA, update
     if visc:
         b2 += 8 * vl + 16 * nE  # vorticity gather, nu / dv, voe
         f2 += 2 * el
@@ -77,13 +77,13 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b2 += 8 * el * T + 8 * cl * T
             f2 += cl * T * Nc
     # ---- K3 cells + vertices
-    b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl + 8 * cl + 8 * nC  # kw, u_next, invArea, h_next, bern, g b
-    f3 = cl * (2 * Nc + 2)
+    b3 = 8 * nE + 8 * el + 8 * nC + 8 * cl  # kw, u_next, invArea, kdiv
+    f3 = cl * (2 * Nc + 1)
     if visc:
         b3 += 8 * slot_c + 8 * nC  # sdv, nu / area
         f3 += cl * Nc
     if T:
-        b3 += 4 * nC + 12 * slot_c + 8 * nE + 8 * cl + 8 * cl * T * 2 + 16 * cl * T + 8 * cl * T * 0.75
+        b3 += 4 * nC + 12 * slot_c + 8 * nE + 8 * cl * 2 + 8 * cl * T * 2 + 16 * cl * T + 8 * cl * T * 0.75
         if fct:
             b3 += 8 * el * T + 16 * cl * T
         if hmix:
