@@ -45,10 +45,22 @@ struct AdjBuffers {
   double *lam_u = nullptr, *lam_h = nullptr, *acc_u = nullptr, *acc_h = nullptr;
   double *lk_u = nullptr, *lk_h = nullptr, *mu_u = nullptr, *mu_h = nullptr;
   double *lhe = nullptr, *lpve = nullptr, *lke = nullptr, *ldiv = nullptr, *lcirc = nullptr, *lhs = nullptr;
+  // the whole reverse sweep, captured once per (N, k, dt) and replayed
+  cudaGraphExec_t rev = nullptr;
+  int rev_N = 0, rev_k = 0;
+  double rev_dt = 0.0;
 };
+
+void drop_adjoint_graph(SwState &s) {
+  if (s.adj && s.adj->rev) {
+    cudaGraphExecDestroy(s.adj->rev);
+    s.adj->rev = nullptr;
+  }
+}
 
 void free_adjoint(SwState &s) {
   if (s.adj) {
+    drop_adjoint_graph(s);
     if (s.adj->arena) cudaFree(s.adj->arena);
     delete s.adj;
     s.adj = nullptr;
@@ -72,6 +84,7 @@ struct AdjArgs {
 
 // R1 (vertices): circ, hs, pv at the stage state.
 __global__ void __launch_bounds__(TPB) k_adj_r1(DMesh m, DStat st, AdjArgs a, int L) {
+  stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nV * L) return;
   const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
@@ -88,6 +101,7 @@ __global__ void __launch_bounds__(TPB) k_adj_r1(DMesh m, DStat st, AdjArgs a, in
 
 // R2 (edges): F, pve, and P = lk_u pve.
 __global__ void __launch_bounds__(TPB) k_adj_r2(DMesh m, AdjArgs a, int L) {
+  stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
@@ -102,6 +116,7 @@ __global__ void __launch_bounds__(TPB) k_adj_r2(DMesh m, AdjArgs a, int L) {
 
 // B1 (edges): transposed PV flux, d tend_h / dF, chain through F = u he.
 __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
+  stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
@@ -127,6 +142,7 @@ __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
 
 // B2 (cells + vertices): gradient terms, h_e -> h, pv -> (circ, hs).
 __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
+  stage_prologue();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
@@ -192,6 +208,7 @@ __device__ __forceinline__ void combine(const AdjArgs &a, int64_t i, double mu, 
 // B3 (cells + edges): thickness through kites; u through circulation, KE and
 // divergence; then the RK combination.
 __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, int L) {
+  stage_prologue();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
@@ -265,11 +282,12 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, const double *u, const double 
   a.lam_u = A.lam_u, a.lam_h = A.lam_h, a.acc_u = A.acc_u, a.acc_h = A.acc_h;
   a.rk = rk, a.visc = s.p.nu != 0.0, a.dt = A.dt, a.g = s.p.gravity, a.nu = s.p.nu;
   const int64_t nE = (int64_t)m.nE * L, nC = (int64_t)m.nC * L, nV = (int64_t)m.nV * L;
-  k_adj_r1<<<blocks_for(nV, TPB), TPB, 0, st>>>(m, s.st, a, L);
-  k_adj_r2<<<blocks_for(nE, TPB), TPB, 0, st>>>(m, a, L);
-  k_adj_b1<<<blocks_for(nE, TPB), TPB, 0, st>>>(m, a, L);
-  k_adj_b2<<<blocks_for(nC + nV, TPB), TPB, 0, st>>>(m, a, L);
-  k_adj_b3<<<blocks_for(nC + nE, TPB), TPB, 0, st>>>(m, s.st, a, L);
+  const bool pdl = s.tune_pdl;
+  launch_pdl(k_adj_r1, nV, TPB, pdl, st, m, s.st, a, L);
+  launch_pdl(k_adj_r2, nE, TPB, pdl, st, m, a, L);
+  launch_pdl(k_adj_b1, nE, TPB, pdl, st, m, a, L);
+  launch_pdl(k_adj_b2, nC + nV, TPB, pdl, st, m, a, L);
+  launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
 }
 
 void forward(SwState &s, double dt, int N, int k) {
@@ -285,7 +303,7 @@ void forward(SwState &s, double dt, int N, int k) {
   MPASO_CUDA(cudaMemcpyAsync(A.ck_h, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
   for (int done = 0, c = 1; done < N; ++c) {
     const int n = std::min(k, N - done);
-    sw_steps_pub(s, dt, n, s.stream);
+    sw_steps_graph(s, dt, n);
     done += n;
     if (done < N) {
       MPASO_CUDA(cudaMemcpyAsync(A.ck_u + (size_t)c * m.nE * s.L, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
@@ -295,7 +313,7 @@ void forward(SwState &s, double dt, int N, int k) {
   A.have_forward = true;
 }
 
-void reverse(SwState &s) {
+void reverse_body(SwState &s) {
   AdjBuffers &A = *s.adj;
   const DMesh &m = s.mesh->ctx.d;
   const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
@@ -322,6 +340,30 @@ void reverse(SwState &s) {
         stage_vjp(s, A, rk, A.tp_u + (size_t)(4 * t + rk) * eu, A.tp_h + (size_t)(4 * t + rk) * ch, st);
   }
   MPASO_CUDA(cudaGetLastError());
+}
+
+// The reverse sweep is ~800 launches per segment of small kernels: captured
+// once as a graph for the current (N, k, dt) and buffers, then replayed.
+void reverse(SwState &s) {
+  AdjBuffers &A = *s.adj;
+  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt)) drop_adjoint_graph(s);
+  if (!A.rev) {
+    cudaGraph_t g;
+    MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      reverse_body(s);
+    } catch (...) {
+      cudaStreamEndCapture(s.stream, &g);
+      cudaGetLastError();
+      throw;
+    }
+    MPASO_CUDA(cudaStreamEndCapture(s.stream, &g));
+    const cudaError_t e = cudaGraphInstantiate(&A.rev, g, 0);
+    cudaGraphDestroy(g);
+    MPASO_CUDA(e);
+    A.rev_N = A.N, A.rev_k = A.k, A.rev_dt = A.dt;
+  }
+  MPASO_CUDA(cudaGraphLaunch(A.rev, s.stream));
   s.diag_valid = false;
 }
 

@@ -38,9 +38,11 @@ constexpr int TPB = 256;
 constexpr int kOccMaxT = 1;  // OC = 1 variants exist up to this many tracers (beyond, they spill)
 #define MPASO_BOUNDS(OC) __launch_bounds__(TPB, (OC) ? 1536 / TPB : 0)
 
+
 // ------------------------------------------------------------- K1: edges
 template <int T, int NW, int OC>
 __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
+  stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
@@ -58,6 +60,7 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
 // ------------------------------------------------------ K2: edges + cells
 template <int T, int NW, int OC>
 __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
+  stage_prologue();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nEL = (int64_t)m.nE * L;
   if (i < nEL) {
@@ -189,6 +192,7 @@ __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, con
 // ------------------------------------------------------ K3: cells + vertices
 template <int T, int NC, int OC>
 __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
+  stage_prologue();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
   const double *u_next = S.stage == 3 ? S.u_new : S.u_out;
@@ -286,6 +290,7 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
 // ------------------------------------------------------------ state context
 SwState::~SwState() {
   if (graph) cudaGraphExecDestroy(graph);
+  if (io_stage) cudaFree(io_stage);
   if (tune_l2) {  // hand the persisting L2 lines back
     cudaCtxResetPersistingL2Cache();
     cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
@@ -362,7 +367,8 @@ Stage make_stage(SwState &s, int rk, double dt) {
 }
 
 // Launch of a stage kernel, with the state's L2 persistence window attached
-// when `win` (the window then travels into captured graphs with the launch).
+// when `win` and programmatic dependent launch when the state enables it
+// (both travel into captured graphs with the launch).
 template <class... A>
 void launch_ex(void (*kern)(A...), int64_t n, int b, bool win, const SwState &s, cudaStream_t st,
                DMesh m, DStat d, Stage S, int L) {
@@ -370,13 +376,18 @@ void launch_ex(void (*kern)(A...), int64_t n, int b, bool win, const SwState &s,
   cfg.gridDim = dim3(blocks_for(n, b));
   cfg.blockDim = dim3(b);
   cfg.stream = st;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
+  unsigned na = 0;
   if (win) {
-    at[0].id = cudaLaunchAttributeAccessPolicyWindow;
-    at[0].val.accessPolicyWindow = s.l2win;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
+    at[na].id = cudaLaunchAttributeAccessPolicyWindow;
+    at[na++].val.accessPolicyWindow = s.l2win;
   }
+  if (s.tune_pdl) {
+    at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[na++].val.programmaticStreamSerializationAllowed = 1;
+  }
+  cfg.attrs = na ? at : nullptr;
+  cfg.numAttrs = na;
   MPASO_CUDA(cudaLaunchKernelEx(&cfg, kern, m, d, S, L));
 }
 
@@ -407,9 +418,9 @@ void launch_k3(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_
   const DMesh &m = s.mesh->ctx.d;
   const int64_t n = ((int64_t)m.nC + m.nV) * s.L;
   if (unroll)
-    k_sw_final<T, 6, OC><<<blocks_for(n, b), b, 0, st>>>(m, s.st, S, s.L);
+    launch_ex(k_sw_final<T, 6, OC>, n, b, false, s, st, m, s.st, S, s.L);
   else
-    k_sw_final<T, 0, OC><<<blocks_for(n, b), b, 0, st>>>(m, s.st, S, s.L);
+    launch_ex(k_sw_final<T, 0, OC>, n, b, false, s, st, m, s.st, S, s.L);
 }
 
 template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st) {
@@ -579,12 +590,40 @@ void time_stage_kernels(SwState &S, double dt, int nsteps, double ms[3]) {
   for (int k = 0; k < nk; ++k) ms[k] = acc[k] / (4.0 * nsteps);
 }
 
+// Device time (ms) of one uninterrupted RK4 step (no events between launches,
+// so launch overlap shows), averaged over nsteps; advances the state.
+double time_whole_steps(SwState &S, double dt, int nsteps) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  float ms = 0.f;
+  try {
+    MPASO_CUDA(cudaEventCreate(&a));
+    MPASO_CUDA(cudaEventCreate(&b));
+    if (S.p.app == MPASO_APP_OCEAN)
+      ocean_prepare(S, dt, S.stream);
+    else
+      ensure_diag(S, S.stream);
+    MPASO_CUDA(cudaEventRecord(a, S.stream));
+    run_steps(S, dt, nsteps, S.stream);
+    MPASO_CUDA(cudaEventRecord(b, S.stream));
+    MPASO_CUDA(cudaEventSynchronize(b));
+    MPASO_CUDA(cudaEventElapsedTime(&ms, a, b));
+  } catch (...) {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    throw;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / nsteps;
+}
+
 // A captured step graph bakes in the launch shapes; drop it when they change.
 void drop_graph(SwState &S) {
   if (S.graph) {
     MPASO_CUDA(cudaGraphExecDestroy(S.graph));
     S.graph = nullptr;
   }
+  drop_adjoint_graph(S);
 }
 
 // Whether kernel k of the stage has a compile-time-unrolled variant on this mesh.
@@ -641,9 +680,30 @@ void get_config(const SwState &S, int32_t *config) {
   for (int k = 0; k < 3; ++k)
     config[k] = S.tune_unroll[k], config[3 + k] = S.tune_tpb[k], config[6 + k] = S.tune_occ[k];
   config[9] = S.tune_l2;
+  config[10] = S.tune_pdl;
 }
 
 constexpr int kTpbChoices[3] = {64, 128, 256};
+
+void step_graph(SwState &S, double dt, int nsteps);
+
+// Device staging for host-memory exchanges (reference order), grown on
+// demand and kept with the state, so repeated calls allocate nothing.
+double *ensure_io(SwState &S, size_t bytes) {
+  if (S.io_bytes < bytes) {
+    if (S.io_stage) {
+      MPASO_CUDA(cudaStreamSynchronize(S.stream));
+      MPASO_CUDA(cudaFree(S.io_stage));
+    }
+    S.io_stage = nullptr, S.io_bytes = 0;
+    if (cudaMalloc((void **)&S.io_stage, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      fail(MPASO_ERR_ALLOC, "device allocation of the host-exchange staging failed");
+    }
+    S.io_bytes = bytes;
+  }
+  return S.io_stage;
+}
 
 }  // namespace
 
@@ -707,14 +767,12 @@ int mpaso_state_set(mpaso_state s, int32_t field, const double *data) {
     MeshCtx &ctx = S.mesh->ctx;
     const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : entity == MPASO_EDGES ? ctx.d.nE : ctx.d.nV;
     const double *src = data;
-    double *stage = nullptr;
     if (!is_device_pointer(data)) {
-      MPASO_CUDA(cudaMallocAsync((void **)&stage, (size_t)n * row * 8, S.stream));
+      double *stage = ensure_io(S, (size_t)n * row * 8);
       MPASO_CUDA(cudaMemcpyAsync(stage, data, (size_t)n * row * 8, cudaMemcpyHostToDevice, S.stream));
       src = stage;
     }
     k_gather_rows_pub(src, buf, ctx.d_perm[entity], n, (int)row, S.stream);
-    if (stage) MPASO_CUDA(cudaFreeAsync(stage, S.stream));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
     S.diag_valid = false;
     S.prep_dt = 0.0;
@@ -733,13 +791,9 @@ int mpaso_state_get(mpaso_state s, int32_t field, double *data) {
     MeshCtx &ctx = S.mesh->ctx;
     const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : entity == MPASO_EDGES ? ctx.d.nE : ctx.d.nV;
     const bool dev = is_device_pointer(data);
-    double *dst = data;
-    if (!dev) MPASO_CUDA(cudaMallocAsync((void **)&dst, (size_t)n * row * 8, S.stream));
+    double *dst = dev ? data : ensure_io(S, (size_t)n * row * 8);
     k_scatter_rows_pub(buf, dst, ctx.d_perm[entity], n, (int)row, S.stream);
-    if (!dev) {
-      MPASO_CUDA(cudaMemcpyAsync(data, dst, (size_t)n * row * 8, cudaMemcpyDeviceToHost, S.stream));
-      MPASO_CUDA(cudaFreeAsync(dst, S.stream));
-    }
+    if (!dev) MPASO_CUDA(cudaMemcpyAsync(data, dst, (size_t)n * row * 8, cudaMemcpyDeviceToHost, S.stream));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
   });
 }
@@ -755,8 +809,74 @@ int mpaso_rk4_step(mpaso_state s, double dt, int32_t nsteps) {
 int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps) {
   return guarded("mpaso_rk4_step_graph", [&] {
     require(s != nullptr && nsteps >= 0, MPASO_ERR_ARG, "bad argument");
+    MPASO_CUDA(cudaSetDevice(s->s.mesh->ctx.device));
+    step_graph(s->s, dt, nsteps);
+  });
+}
+
+int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                        double *tracers) {
+  return guarded("mpaso_rk4_step_host", [&] {
+    require(s && h && u && nsteps >= 0, MPASO_ERR_ARG, "bad argument");
     SwState &S = s->s;
-    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    MeshCtx &ctx = S.mesh->ctx;
+    MPASO_CUDA(cudaSetDevice(ctx.device));
+    const int64_t nC = ctx.d.nC, nE = ctx.d.nE, L = S.L;
+    const bool tr = tracers != nullptr && S.T > 0;
+    const int64_t nh = nC * L, nu = nE * L, nt = tr ? nC * L * S.T : 0;
+    const cudaStream_t st = S.stream;
+    // Page-locked host buffers the device can address (UVA) are read and written
+    // by the permutation kernels directly over the host link: no staging copies.
+    const double *hp[3] = {h, u, tracers};
+    double *mapped[3] = {nullptr, nullptr, nullptr};
+    bool all_mapped = true;
+    for (int f = 0; f < (tr ? 3 : 2); ++f) {
+      cudaPointerAttributes a;
+      if (cudaPointerGetAttributes(&a, hp[f]) != cudaSuccess) cudaGetLastError();
+      else if (a.type == cudaMemoryTypeHost && a.devicePointer) mapped[f] = (double *)a.devicePointer;
+      all_mapped = all_mapped && mapped[f];
+    }
+    if (all_mapped) {
+      k_gather_rows_pub(mapped[0], S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+      k_gather_rows_pub(mapped[1], S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+      if (tr) k_gather_rows_pub(mapped[2], S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+      S.diag_valid = false;
+      S.prep_dt = 0.0;
+      step_graph(S, dt, nsteps);
+      k_scatter_rows_pub(S.H[0], mapped[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+      k_scatter_rows_pub(S.U[0], mapped[1], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+      if (tr) k_scatter_rows_pub(S.TR0, mapped[2], ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+      MPASO_CUDA(cudaStreamSynchronize(st));
+      return;
+    }
+    const size_t bytes = (size_t)(nh + nu + nt) * sizeof(double);
+    double *dh = ensure_io(S, bytes), *du = dh + nh, *dtr = du + nu;
+    // pageable memory: one copy per field each way, permutations on the device, one synchronisation
+    MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
+    MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (tr) MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+    k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+    if (tr) k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+    S.diag_valid = false;
+    S.prep_dt = 0.0;
+    step_graph(S, dt, nsteps);
+    k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+    k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+    if (tr) k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+    MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (tr) MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MPASO_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+}  // extern "C"
+
+namespace {
+// Graph-replayed RK4 steps (the body of mpaso_rk4_step_graph).
+void step_graph(SwState &S, double dt, int nsteps) {
+  {
     if (S.p.app == MPASO_APP_SW)
       ensure_diag(S, S.stream);
     else
@@ -781,20 +901,15 @@ int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps) {
       S.graph_dt = dt;
     }
     for (int n = 0; n < nsteps; ++n) MPASO_CUDA(cudaGraphLaunch(S.graph, S.stream));
-  });
+  }
 }
+}  // namespace
 
-int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
-                        double *tracers) {
-  int rc = mpaso_state_set(s, MPASO_FIELD_H, h);
-  if (!rc) rc = mpaso_state_set(s, MPASO_FIELD_U, u);
-  if (!rc && tracers && s->s.T > 0) rc = mpaso_state_set(s, MPASO_FIELD_TRACERS, tracers);
-  if (!rc) rc = mpaso_rk4_step_graph(s, dt, nsteps);
-  if (!rc) rc = mpaso_state_get(s, MPASO_FIELD_H, h);
-  if (!rc) rc = mpaso_state_get(s, MPASO_FIELD_U, u);
-  if (!rc && tracers && s->s.T > 0) rc = mpaso_state_get(s, MPASO_FIELD_TRACERS, tracers);
-  return rc;
-}
+namespace mpaso {
+void sw_steps_graph(SwState &s, double dt, int nsteps) { step_graph(s, dt, nsteps); }
+}  // namespace mpaso
+
+extern "C" {
 
 int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per_launch,
                         int32_t *nkinds, char *names, int32_t names_len) {
@@ -858,6 +973,7 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
       require(config[6 + k] == 0 || config[6 + k] == 1, MPASO_ERR_ARG, "occupancy flag must be 0 or 1");
     }
     require(config[9] >= 0 && config[9] <= 2, MPASO_ERR_ARG, "L2 window choice must be 0, 1 or 2");
+    require(config[10] == 0 || config[10] == 1, MPASO_ERR_ARG, "launch overlap flag must be 0 or 1");
     SwState &S = s->s;
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
@@ -865,6 +981,7 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
     for (int k = 0; k < 3; ++k)
       S.tune_unroll[k] = config[k], S.tune_tpb[k] = config[3 + k], S.tune_occ[k] = config[6 + k];
     set_l2_window(S, config[9]);
+    S.tune_pdl = config[10];
   });
 }
 
@@ -929,6 +1046,18 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
         if (tot < 0.98 * best) best = tot, best_l2 = w;  // keep the simpler choice unless clearly faster
       }
       set_l2_window(S, best_l2);
+      // programmatic dependent launch (sw stage kernels), judged on uninterrupted steps
+      if (S.p.app == MPASO_APP_SW) {
+        double t[2];
+        for (int pdl = 0; pdl <= 1; ++pdl) {
+          S.tune_pdl = pdl;
+          save_restore(false);
+          time_whole_steps(S, dt, 1);
+          save_restore(false);
+          t[pdl] = time_whole_steps(S, dt, nsteps);
+        }
+        S.tune_pdl = t[0] < 0.98 * t[1] ? 0 : 1;
+      }
       save_restore(false);
       MPASO_CUDA(cudaStreamSynchronize(S.stream));
     } catch (...) {

@@ -25,6 +25,34 @@ __device__ __forceinline__ double rcp_nr(double b) {
 
 __device__ __forceinline__ long long sign_mask(double s) { return dbits(s) & kSignBit; }
 
+// Programmatic dependent launch: a kernel launched with the
+// programmatic-serialization attribute may be scheduled while its
+// predecessor's last blocks still run; it waits here (a hardware dependency,
+// no polling) until the predecessor has completed and its writes are
+// visible, then lets its own successor start launching.  Without the
+// attribute both instructions return at once.  Every kernel launched with
+// the attribute starts with this, before touching memory.
+__device__ __forceinline__ void stage_prologue() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch with programmatic dependent launch when `pdl` (the attribute travels
+// into captured graphs).
+template <class... K, class... A>
+void launch_pdl(void (*kern)(K...), int64_t n, int threads, bool pdl, cudaStream_t st, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks_for(n, threads));
+  cfg.blockDim = dim3(threads);
+  cfg.stream = st;
+  cudaLaunchAttribute at;
+  at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at.val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = pdl ? &at : nullptr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  MPASO_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 // Per-state derived statics (device arrays), built once at state creation.
 // The sw kernels carry the doubled thickness flux F2 = u (h1 + h2) = 2 F and
 // the doubled edge PV Pv = pv_a + pv_b = 2 pv_e; the power-of-two factors are
@@ -86,6 +114,9 @@ struct SwState {
   double prep_dt = 0.0;     // ocean: dt of the cached F / 1/hProv (0 = stale)
   cudaGraphExec_t graph = nullptr;
   double graph_dt = 0.0;
+  // device staging of mpaso_rk4_step_host (reference-ordered h, u, tracers)
+  double *io_stage = nullptr;
+  size_t io_bytes = 0;
   // optional per-launch timing: events recorded after every kernel of a stage
   cudaEvent_t *prof_events = nullptr;
   // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu
@@ -101,6 +132,8 @@ struct SwState {
   // window is attached to that kernel's launches (see set_l2_window)
   int tune_l2 = 0;
   cudaAccessPolicyWindow l2win{};
+  // stage kernels launched with programmatic dependent launch (sw app)
+  int tune_pdl = 1;
   ~SwState();
 };
 
@@ -114,6 +147,9 @@ void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const doub
                    double *u_acc, double *h_acc, double *u_new, double *h_new, cudaStream_t st);
 void sw_diag_ptrs(SwState &s, const double *u, const double *h, cudaStream_t st);
 void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
+// nsteps graph-replayed steps on the state's stream (the step graph is cached)
+void sw_steps_graph(SwState &s, double dt, int nsteps);
+void drop_adjoint_graph(SwState &s);
 
 // ---------------------------------------------------------------------------
 // FCT / del2 tracer device code (apps/ocean/tasks/solve.cc:99-366).

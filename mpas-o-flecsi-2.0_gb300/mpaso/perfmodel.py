@@ -3,9 +3,12 @@
 Bytes: every array a launch touches counted once (reads + writes), at its
 real size on the mesh (8 B per double, 4 B per index), the compulsory traffic
 of the dataflow -- repeated gathers of a neighbour's value are not counted
-again.  FP64 work: DADD / DMUL / DFMA instructions per launch (a division by
-rcp_nr is 5 instructions plus one multiply); min/max/select/sign work runs on
-the integer pipe and is not counted.
+again.  FP64 work: DADD / DMUL / DFMA thread instructions per launch (a
+reciprocal by rcp_nr is 4 on the FP64 pipe plus the approximation on the
+special-function unit; the limiter's two guarded quotients run only where a
+bound is active, counted as a quarter of the cells); min/max/select/sign work
+runs on the integer pipe and is not counted.  ncu's counts for the same
+launches are in profiles/ (within about 10% of these).
 
 One cell-update = one cell x one level advanced by one full RK4 step.
 """
@@ -49,7 +52,8 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             # advCells + the one coefficient the flux sign selects (the {cp, cm} pair the kernel
             # loads is 8 B more per slot), hoMask, LO, A
             b1 += 12 * Na * nE + 4 * el + 16 * el * T
-            f1 += el * T * (Na + 3)
+            # stencil sum, LO, HO, A and the centred fallback (selected, not branched) per tracer
+            f1 += el * (1 + T * (Na + 5))
         else:
             b1 += 8 * el * T
             f1 += el * (1 + 2 * T)
@@ -70,9 +74,9 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
         b2 += 8 * slot_c
         if fct:
             b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
-            # 1/hProv (6), dt/area, dt/(area hProv); per tracer 3 sums per edge, trUp (3),
-            # numerators / denominators (4), two guarded quotients (12)
-            f2 += cl * (8 + T * (3 * Nc + 19))
+            # 1/hProv (5), dt/area, dt/(area hProv); per tracer 3 sums per edge, trUp (3),
+            # numerators / denominators (4), two guarded quotients (10, a quarter of the cells)
+            f2 += cl * (7 + T * (3 * Nc + 7 + 2.5))
         else:
             b2 += 8 * el * T + 8 * cl * T
             f2 += cl * T * Nc
@@ -88,9 +92,10 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b3 += 8 * el * T + 16 * cl * T
         if hmix:
             b3 += 8 * el * T
-        f3 += cl * (5 + T * (Nc * (1 + int(fct) + int(hmix)) + 4.75))
+        # per slot: a r - DF contracts to one FMA, plus the accumulation
+        f3 += cl * (4 + T * (Nc * (1 + int(fct)) + 4.75))
     b3 += 8 * nV * (3 + 1.5 + 3 + 1.5 + 3) + 8 * vl + 16 * vl
-    f3 += vl * 14  # circulation and kite sums (6), vorticity, f A + circ, 1/hs (5), pv
+    f3 += vl * 13  # circulation and kite sums (6), vorticity, f A + circ, 1/hs (4), pv
     return {"sw_edge_pre": (b1, f1), "sw_tend": (b2, f2), "sw_final": (b3, f3)}
 
 
@@ -104,16 +109,16 @@ def ocean_kernels(d: Dims, fct=True, hmix=True):
     f1 = el
     if fct:
         b1 += 12 * Na * nE + 4 * el + 16 * el * T
-        f1 += el * T * (Na + 3)
+        f1 += el * (1 + T * (Na + 5))
     if hmix:
         b1 += 8 * nE + 8 * el * T
         f1 += el * (1 + 2 * T)
     b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
     b2 += 16 * el * T + 24 * cl * T
-    f2 = cl * (2 + T * (3 * Nc + 19))
+    f2 = cl * (2 + T * (3 * Nc + 7 + 2.5))
     b3 = 4 * nC + 12 * slot_c + 8 * nC + 8 * nE + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
     b3 += 8 * el * T * (int(fct) + int(hmix))
-    f3 = cl * T * (Nc * (1 + int(fct) + int(hmix)) + 2.75)
+    f3 = cl * T * (Nc * (1 + int(fct)) + 2.75)
     return {"oc_edges": (b1, f1), "oc_cells": (b2, f2), "oc_final": (b3, f3)}
 
 

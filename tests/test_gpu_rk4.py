@@ -163,3 +163,18 @@ def test_del2_mode_decay_on_device():
     a = float((got[1][:, 0] * pattern).sum() / (pattern * pattern).sum()) / 1e-6
     assert abs(-np.log(a) / (nu * dt * n) / k2 - 1) < 0.01
     assert rel_max(got[1], want[1]) < TOL100
+
+
+def test_host_boundary_call_with_page_locked_buffers():
+    """Page-locked (mapped) host buffers take the zero-copy path of mpaso_rk4_step_host;
+    it must give exactly what the staged path gives for pageable buffers."""
+    torch = pytest.importorskip("torch")
+    import mpaso.gpu as G
+    g = Golden("sw_fct_icosa3_L1T1")
+    _, st = make_state(g)
+    h, u, tr = g["h0"].copy(), g["u0"].copy(), g["tr0"].copy()
+    st.step_host(g.dt, 2, h, u, tr)
+    _, st2 = make_state(g)
+    hp, up, tp = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (g["h0"], g["u0"], g["tr0"]))
+    st2.step_host(g.dt, 2, hp, up, tp)
+    assert np.array_equal(hp.numpy(), h) and np.array_equal(up.numpy(), u) and np.array_equal(tp.numpy(), tr)
