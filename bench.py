@@ -364,8 +364,8 @@ def adjoint_arm(args):
                        "loss": "0.5 * sum(area (h_N - h_target)^2) / sum(area)"},
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp,
             "vjp_over_plain_forward": t_vjp / t_plain,
-            "fd_check": {"directions": args.adj_dirs, "max_rel_err": max(errs),
-                         "median_rel_err": float(np.median(errs))},
+            "fd_check": {"directions": args.adj_dirs, "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None},
             "peak_device_bytes": int(mem)}
 
 

@@ -275,7 +275,9 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
  * state before it into gh0 / gu0 (reference ordering; host or device
  * pointers).  Stage states are recomputed segment by segment from the
  * checkpoints.  Device memory: ceil(N / ckpt_every) + 4 ckpt_every + 2
- * copies of (h, u) plus about 20 work arrays of one level-field each. */
+ * copies of (h, u), 4 ckpt_every + 1 copies of two vertex fields (the taped
+ * pv and kite-summed thickness), and about 20 work arrays of one level-field
+ * each. */
 int mpaso_rk4_forward(mpaso_state s, double dt, int32_t nsteps, int32_t ckpt_every);
 int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0, double *gu0);
 int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);

@@ -41,7 +41,9 @@ struct AdjBuffers {
   double *ck_u = nullptr, *ck_h = nullptr;  // checkpoints [nck][nE L], [nck][nC L]
   double *tp_u = nullptr, *tp_h = nullptr;  // stage-state tape [4k + 1][...]
   double *uacc = nullptr, *hacc = nullptr;
-  double *pv = nullptr, *hs = nullptr, *F = nullptr, *pve = nullptr, *P = nullptr;
+  double *tp_pv = nullptr, *tp_hs = nullptr;  // pv, kite-summed h of every tape slot [4k + 1][nV L]
+  double *pve = nullptr;
+  double2 *FP = nullptr;  // {F, P} per edge, gathered together by B1
   double *lam_u = nullptr, *lam_h = nullptr, *acc_u = nullptr, *acc_h = nullptr;
   double *lk_u = nullptr, *lk_h = nullptr, *mu_u = nullptr, *mu_h = nullptr;
   double *lhe = nullptr, *lpve = nullptr, *lke = nullptr, *ldiv = nullptr, *lcirc = nullptr, *lhs = nullptr;
@@ -73,7 +75,11 @@ constexpr int TPB = 256;
 
 struct AdjArgs {
   const double *u, *h;                        // stage state
-  double *pv, *hs, *F, *pve, *P;              // recomputed forward quantities
+  const double *pv, *hs;                      // taped pv, kite-summed h of the stage state
+  double *pve;                                // edge pv of the stage state
+  double2 *FP;                                // {F = u he, P = lk_u pve} per edge
+  const double *un, *hn, *pvn;                // state of the next stage to reverse (prep)
+  int prep;                                   // B3 prepares FP, pve of that stage
   double *lk_u, *lk_h;                        // cotangent of the stage tendency (in), next one (out)
   double *mu_u, *mu_h;                        // J^T lk
   double *lhe, *lpve, *lke, *ldiv, *lcirc, *lhs;
@@ -82,57 +88,52 @@ struct AdjArgs {
   double dt, g, nu;
 };
 
-// R1 (vertices): circ, hs, pv at the stage state.
-__global__ void __launch_bounds__(TPB) k_adj_r1(DMesh m, DStat st, AdjArgs a, int L) {
-  stage_prologue();
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= (int64_t)m.nV * L) return;
-  const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
-  double circ = 0.0, hs = 0.0;
-#pragma unroll
-  for (int j = 0; j < kVertexDegree; ++j) {
-    const int64_t s = (int64_t)j * m.nV + v;
-    circ = fma(st.sdc[s], a.u[(int64_t)m.eov[s] * L + k], circ);
-    hs = fma(m.kite[s], a.h[(int64_t)m.cov[s] * L + k], hs);
-  }
-  a.hs[i] = hs;
-  a.pv[i] = fma(m.fVertex[v], m.areaTriangle[v], circ) * rcp_nr(hs);
+// Edge quantities of a stage state that B1 gathers: F = u he, pve from the taped
+// vertex pv, and P = lk_u pve (lk_u: the stage tendency's cotangent).
+__device__ __forceinline__ void prep_edge(const DMesh &m, const AdjArgs &a, int L, int e, int k, int64_t i,
+                                          const double *u, const double *h, const double *pv, double lk) {
+  const int2 c = m.coe[e];
+  const int2 v = m.voe[e];
+  const double he = 0.5 * (h[(int64_t)c.x * L + k] + h[(int64_t)c.y * L + k]);
+  const double pve = 0.5 * (pv[(int64_t)v.x * L + k] + pv[(int64_t)v.y * L + k]);
+  a.pve[i] = pve;
+  a.FP[i] = make_double2(u[i] * he, lk * pve);
 }
 
-// R2 (edges): F, pve, and P = lk_u pve.
-__global__ void __launch_bounds__(TPB) k_adj_r2(DMesh m, AdjArgs a, int L) {
+// PREP (edges): the above for the first stage reversed in a segment (later
+// stages get it from the B3 before them).
+__global__ void __launch_bounds__(TPB) k_adj_prep(DMesh m, AdjArgs a, int L) {
   stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
-  const int2 c = m.coe[e];
-  const int2 v = m.voe[e];
-  const double he = 0.5 * (a.h[(int64_t)c.x * L + k] + a.h[(int64_t)c.y * L + k]);
-  a.F[i] = a.u[i] * he;
-  const double pve = 0.5 * (a.pv[(int64_t)v.x * L + k] + a.pv[(int64_t)v.y * L + k]);
-  a.pve[i] = pve;
-  a.P[i] = a.lk_u[i] * pve;
+  prep_edge(m, a, L, e, k, i, a.u, a.h, a.pv, a.lk_u[i]);
 }
 
 // B1 (edges): transposed PV flux, d tend_h / dF, chain through F = u he.
+// NW = 10: the edgesOnEdge stencil unrolled at compile time (10-slot meshes).
+template <int NW>
 __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
   stage_prologue();
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
   double s1 = 0.0, t1 = 0.0, t2 = 0.0;
-  for (int j = 0; j < m.maxEoE; ++j) {
+  const int ne = NW > 0 ? NW : m.maxEoE;
+#pragma unroll
+  for (int j = 0; j < ne; ++j) {
     const int64_t s = (int64_t)j * m.nE + e;
     const int64_t io = (int64_t)m.eoe[s] * L + k;
     const double wt = m.woeT[s];
-    s1 = fma(m.woe[s], a.F[io], s1);
+    const double2 fp = a.FP[io];
+    s1 = fma(m.woe[s], fp.x, s1);
     t1 = fma(wt, a.lk_u[io], t1);
-    t2 = fma(wt, a.P[io], t2);
+    t2 = fma(wt, fp.y, t2);
   }
   const int2 c = m.coe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
   const double he = 0.5 * (a.h[i1] + a.h[i2]);
-  const double Fe = a.F[i], pve = a.pve[i], ue = a.u[i];
+  const double Fe = a.FP[i].x, pve = a.pve[i], ue = a.u[i];
   const double dth = a.lk_h[i2] * m.invAreaCell[c.y] - a.lk_h[i1] * m.invAreaCell[c.x];
   const double lF = fma(0.5, fma(pve, t1, t2), m.dvEdge[e] * dth);
   a.lpve[i] = 0.5 * fma(a.lk_u[i], s1, Fe * t1);
@@ -147,14 +148,18 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    const int n = m.nEoC[c];
     double G = 0.0, sl = 0.0;
-    for (int j = 0; j < n; ++j) {
-      const int e = m.eoc[(int64_t)j * m.nC + c];
+    auto slot = [&](int j, bool ok) {
+      const int64_t s = (int64_t)j * m.nC + c;
+      const int e = m.eoc[s];
       const int64_t ie = (int64_t)e * L + k;
-      G += dflip(m.invDcEdge[e] * a.lk_u[ie], sign_mask(m.eocSign[(int64_t)j * m.nC + c]));
-      sl += a.lhe[ie];
-    }
+      G += dmask(dflip(m.invDcEdge[e] * a.lk_u[ie], sign_mask(m.eocSign[s])), ok);
+      sl += dmask(a.lhe[ie], ok);
+    };
+    if (m.maxEoC <= 6)
+      for_slots<6>(m.nEoC[c], slot);
+    else
+      for_slots<0>(m.nEoC[c], slot);
     a.mu_h[i] = fma(0.5, sl, -a.g * G);
     a.lke[i] = -G;
     if (a.visc) a.ldiv[i] = a.nu * G;
@@ -181,28 +186,31 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
 }
 
 // RK4 cotangent bookkeeping for one element once mu is complete.
-__device__ __forceinline__ void combine(const AdjArgs &a, int64_t i, double mu, double *lam, double *acc,
-                                        double *lk) {
+__device__ __forceinline__ double combine(const AdjArgs &a, int64_t i, double mu, double *lam, double *acc,
+                                          double *lk) {
   const double dt = a.dt;
+  double l;
   switch (a.rk) {
     case 3:
       acc[i] = lam[i] + mu;
-      lk[i] = fma(dt, mu, (dt / 3) * lam[i]);
+      l = fma(dt, mu, (dt / 3) * lam[i]);
       break;
     case 2:
       acc[i] += mu;
-      lk[i] = fma(dt / 2, mu, (dt / 3) * lam[i]);
+      l = fma(dt / 2, mu, (dt / 3) * lam[i]);
       break;
     case 1:
       acc[i] += mu;
-      lk[i] = fma(dt / 2, mu, (dt / 6) * lam[i]);
+      l = fma(dt / 2, mu, (dt / 6) * lam[i]);
       break;
     default: {
       const double ln = acc[i] + mu;
       lam[i] = ln;
-      lk[i] = (dt / 6) * ln;
+      l = (dt / 6) * ln;
     }
   }
+  lk[i] = l;
+  return l;
 }
 
 // B3 (cells + edges): thickness through kites; u through circulation, KE and
@@ -232,7 +240,9 @@ __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, in
   mu = fma(m.dcEdge[e], a.lcirc[(int64_t)v.y * L + k] - a.lcirc[(int64_t)v.x * L + k], mu);
   mu = fma(2.0 * a.u[i] * st.kw[e], fma(a.lke[i1], ia1, a.lke[i2] * ia2), mu);
   if (a.visc) mu = fma(-m.dvEdge[e], fma(a.ldiv[i2], ia2, -a.ldiv[i1] * ia1), mu);
-  combine(a, i, mu, a.lam_u, a.acc_u, a.lk_u);
+  const double lk = combine(a, i, mu, a.lam_u, a.acc_u, a.lk_u);
+  // the next stage's B1 inputs (B1 of this stage has completed)
+  if (a.prep) prep_edge(m, a, L, e, k, i, a.un, a.hn, a.pvn, lk);
 }
 
 __global__ void k_adj_init(int64_t n, const double *lam, double *lk, double c) {
@@ -250,8 +260,9 @@ void ensure_buffers(SwState &s, int N, int k) {
   A = s.adj = new AdjBuffers();
   std::vector<std::pair<double **, int64_t>> bufs = {
       {&A->ck_u, nck * eu}, {&A->ck_h, nck * ch}, {&A->tp_u, (4LL * k + 1) * eu},
-      {&A->tp_h, (4LL * k + 1) * ch}, {&A->uacc, eu}, {&A->hacc, ch}, {&A->pv, vv}, {&A->hs, vv},
-      {&A->F, eu}, {&A->pve, eu}, {&A->P, eu}, {&A->lam_u, eu}, {&A->lam_h, ch}, {&A->acc_u, eu},
+      {&A->tp_h, (4LL * k + 1) * ch}, {&A->uacc, eu}, {&A->hacc, ch}, {&A->tp_pv, (4LL * k + 1) * vv},
+      {&A->tp_hs, (4LL * k + 1) * vv},
+      {(double **)&A->FP, 2 * eu}, {&A->pve, eu}, {&A->lam_u, eu}, {&A->lam_h, ch}, {&A->acc_u, eu},
       {&A->acc_h, ch}, {&A->lk_u, eu}, {&A->lk_h, ch}, {&A->mu_u, eu}, {&A->mu_h, ch}, {&A->lhe, eu},
       {&A->lpve, eu}, {&A->lke, ch}, {&A->ldiv, ch}, {&A->lcirc, vv}, {&A->lhs, vv}};
   size_t total = 0;
@@ -272,20 +283,32 @@ void ensure_buffers(SwState &s, int N, int k) {
   A->cap_k = k;
 }
 
-void stage_vjp(SwState &s, AdjBuffers &A, int rk, const double *u, const double *h, cudaStream_t st) {
+// Reverse of the stage whose input state is tape slot j; `first`: no B3 before
+// it prepared its edge quantities; `prep_next`: prepare those of slot j - 1.
+void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_next, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
+  const int64_t nE = (int64_t)m.nE * L, nC = (int64_t)m.nC * L, nV = (int64_t)m.nV * L;
   AdjArgs a{};
-  a.u = u, a.h = h, a.pv = A.pv, a.hs = A.hs, a.F = A.F, a.pve = A.pve, a.P = A.P;
+  a.u = A.tp_u + (size_t)j * nE, a.h = A.tp_h + (size_t)j * nC;
+  a.pv = A.tp_pv + (size_t)j * nV, a.hs = A.tp_hs + (size_t)j * nV;
+  a.FP = A.FP, a.pve = A.pve;
   a.lk_u = A.lk_u, a.lk_h = A.lk_h, a.mu_u = A.mu_u, a.mu_h = A.mu_h;
   a.lhe = A.lhe, a.lpve = A.lpve, a.lke = A.lke, a.ldiv = A.ldiv, a.lcirc = A.lcirc, a.lhs = A.lhs;
   a.lam_u = A.lam_u, a.lam_h = A.lam_h, a.acc_u = A.acc_u, a.acc_h = A.acc_h;
   a.rk = rk, a.visc = s.p.nu != 0.0, a.dt = A.dt, a.g = s.p.gravity, a.nu = s.p.nu;
-  const int64_t nE = (int64_t)m.nE * L, nC = (int64_t)m.nC * L, nV = (int64_t)m.nV * L;
-  const bool pdl = s.tune_pdl;
-  launch_pdl(k_adj_r1, nV, TPB, pdl, st, m, s.st, a, L);
-  launch_pdl(k_adj_r2, nE, TPB, pdl, st, m, a, L);
-  launch_pdl(k_adj_b1, nE, TPB, pdl, st, m, a, L);
+  a.prep = prep_next ? 1 : 0;
+  if (prep_next) {
+    a.un = A.tp_u + (size_t)(j - 1) * nE, a.hn = A.tp_h + (size_t)(j - 1) * nC;
+    a.pvn = A.tp_pv + (size_t)(j - 1) * nV;
+  }
+  // plain stream order: programmatic dependent launch made this 25% slower (measured)
+  const bool pdl = false;
+  if (first) launch_pdl(k_adj_prep, nE, TPB, pdl, st, m, a, L);
+  if (m.maxEoE == 10)
+    launch_pdl(k_adj_b1<10>, nE, TPB, pdl, st, m, a, L);
+  else
+    launch_pdl(k_adj_b1<0>, nE, TPB, pdl, st, m, a, L);
   launch_pdl(k_adj_b2, nC + nV, TPB, pdl, st, m, a, L);
   launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
 }
@@ -325,19 +348,24 @@ void reverse_body(SwState &s) {
     // taping recompute of the segment: slot 4t + rk holds the input of stage rk of step s0 + t
     MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
     MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
-    sw_diag_ptrs(s, A.tp_u, A.tp_h, st);
+    const int64_t vv = (int64_t)m.nV * s.L;
+    sw_diag_ptrs(s, A.tp_u, A.tp_h, A.tp_pv, A.tp_hs, st);
     for (int t = 0; t < n; ++t) {
       double *yu = A.tp_u + (size_t)4 * t * eu, *yh = A.tp_h + (size_t)4 * t * ch;
       for (int rk = 0; rk < 4; ++rk) {
         double *iu = yu + (size_t)rk * eu, *ih = yh + (size_t)rk * ch;
         double *ou = yu + (size_t)(rk + 1) * eu, *oh = yh + (size_t)(rk + 1) * ch;
+        const size_t next = (size_t)(4 * t + rk + 1) * vv;  // tape slot of the stage's output
         sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc,
-                      A.hacc, rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, st);
+                      A.hacc, rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next,
+                      A.tp_hs + next, st);
       }
     }
     for (int t = n - 1; t >= 0; --t)
-      for (int rk = 3; rk >= 0; --rk)
-        stage_vjp(s, A, rk, A.tp_u + (size_t)(4 * t + rk) * eu, A.tp_h + (size_t)(4 * t + rk) * ch, st);
+      for (int rk = 3; rk >= 0; --rk) {
+        const int j = 4 * t + rk;
+        stage_vjp(s, A, rk, j, t == n - 1 && rk == 3, j > 0, st);
+      }
   }
   MPASO_CUDA(cudaGetLastError());
 }

@@ -186,7 +186,9 @@ __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, con
   }
   S.vort[i] = circ * m.invAreaTriangle[v];
   // (f + circ/A) / (hs/A) = (f A + circ) / hs
-  S.pv[i] = fma(m.fVertex[v], m.areaTriangle[v], circ) * rcp_nr(hs);
+  const double pv = fma(m.fVertex[v], m.areaTriangle[v], circ) * rcp_nr(hs);
+  S.pv[i] = pv;
+  if (S.tape_pv) S.tape_pv[i] = pv, S.tape_hs[i] = hs;
 }
 
 // ------------------------------------------------------ K3: cells + vertices
@@ -504,21 +506,28 @@ void sw_create(SwState &s) {
 
 // One RK stage of (h, u) only, on explicit buffers (the adjoint's taping
 // recompute).  Tracers are passive in the sw app, so they are left out.
+// tape_pv / tape_hs (may be null) receive pv and the kite-summed thickness of
+// the stage's output state.
 void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
                    const double *u_prev, const double *h_prev, double *u_out, double *h_out,
-                   double *u_acc, double *h_acc, double *u_new, double *h_new, cudaStream_t st) {
+                   double *u_acc, double *h_acc, double *u_new, double *h_new, double *tape_pv,
+                   double *tape_hs, cudaStream_t st) {
   Stage S = make_stage(s, rk, dt);
   S.u_in = u_in, S.h_in = h_in, S.u_prev = u_prev, S.h_prev = h_prev;
   S.u_out = u_out, S.h_out = h_out, S.u_acc = u_acc, S.h_acc = h_acc, S.u_new = u_new, S.h_new = h_new;
   S.fct = 0, S.hmix = 0;
+  S.tape_pv = tape_pv, S.tape_hs = tape_hs;
   launch_stage_T<0>(s, S, st);
 }
 
-// Diagnostics (pv, vorticity, ke, divergence) of an explicit (u, h).
-void sw_diag_ptrs(SwState &s, const double *u, const double *h, cudaStream_t st) {
+// Diagnostics (pv, vorticity, ke, divergence) of an explicit (u, h); pv and the
+// kite-summed thickness also go to tape_pv / tape_hs when given.
+void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv, double *tape_hs,
+                  cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   Stage S = make_stage(s, 0, 0.0);
   S.u_in = u, S.h_in = h;
+  S.tape_pv = tape_pv, S.tape_hs = tape_hs;
   k_sw_diag<<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
 }
 
@@ -825,33 +834,12 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
     const bool tr = tracers != nullptr && S.T > 0;
     const int64_t nh = nC * L, nu = nE * L, nt = tr ? nC * L * S.T : 0;
     const cudaStream_t st = S.stream;
-    // Page-locked host buffers the device can address (UVA) are read and written
-    // by the permutation kernels directly over the host link: no staging copies.
-    const double *hp[3] = {h, u, tracers};
-    double *mapped[3] = {nullptr, nullptr, nullptr};
-    bool all_mapped = true;
-    for (int f = 0; f < (tr ? 3 : 2); ++f) {
-      cudaPointerAttributes a;
-      if (cudaPointerGetAttributes(&a, hp[f]) != cudaSuccess) cudaGetLastError();
-      else if (a.type == cudaMemoryTypeHost && a.devicePointer) mapped[f] = (double *)a.devicePointer;
-      all_mapped = all_mapped && mapped[f];
-    }
-    if (all_mapped) {
-      k_gather_rows_pub(mapped[0], S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
-      k_gather_rows_pub(mapped[1], S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
-      if (tr) k_gather_rows_pub(mapped[2], S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
-      S.diag_valid = false;
-      S.prep_dt = 0.0;
-      step_graph(S, dt, nsteps);
-      k_scatter_rows_pub(S.H[0], mapped[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
-      k_scatter_rows_pub(S.U[0], mapped[1], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
-      if (tr) k_scatter_rows_pub(S.TR0, mapped[2], ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
-      MPASO_CUDA(cudaStreamSynchronize(st));
-      return;
-    }
     const size_t bytes = (size_t)(nh + nu + nt) * sizeof(double);
     double *dh = ensure_io(S, bytes), *du = dh + nh, *dtr = du + nu;
-    // pageable memory: one copy per field each way, permutations on the device, one synchronisation
+    // one copy per field each way (copy engines; page-locked buffers go at link speed),
+    // the permutations on the device, one synchronisation.  (Letting the permutation
+    // kernels read and write mapped host memory directly was slower: their accesses
+    // are scattered.)
     MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
     MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, st));
     if (tr) MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, st));

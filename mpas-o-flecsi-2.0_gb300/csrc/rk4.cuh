@@ -93,6 +93,7 @@ struct Stage {
   double2 *R2;                              // {R+, R-} limiter factors per cell and tracer
   double *tLO;                              // cell intermediates
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
+  double *tape_pv, *tape_hs;                // adjoint taping: pv and kite-summed h of the next state
 };
 
 // State context (sw or ocean app).
@@ -132,8 +133,9 @@ struct SwState {
   // window is attached to that kernel's launches (see set_l2_window)
   int tune_l2 = 0;
   cudaAccessPolicyWindow l2win{};
-  // stage kernels launched with programmatic dependent launch (sw app)
-  int tune_pdl = 1;
+  // stage kernels launched with programmatic dependent launch (sw app; off
+  // unless the autotuner measures it faster)
+  int tune_pdl = 0;
   ~SwState();
 };
 
@@ -144,8 +146,10 @@ void stat_buffers(SwState &s, std::vector<std::pair<double **, int64_t>> &bufs);
 void free_adjoint(SwState &s);
 void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
                    const double *u_prev, const double *h_prev, double *u_out, double *h_out,
-                   double *u_acc, double *h_acc, double *u_new, double *h_new, cudaStream_t st);
-void sw_diag_ptrs(SwState &s, const double *u, const double *h, cudaStream_t st);
+                   double *u_acc, double *h_acc, double *u_new, double *h_new, double *tape_pv,
+                   double *tape_hs, cudaStream_t st);
+void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv, double *tape_hs,
+                  cudaStream_t st);
 void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
 // nsteps graph-replayed steps on the state's stream (the step graph is cached)
 void sw_steps_graph(SwState &s, double dt, int nsteps);

@@ -292,7 +292,7 @@ class State:
         check(lib().mpaso_state_launch_config(self._h, c))
         return self._cfg_dict(c)
 
-    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=1):
+    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=0):
         c = (ctypes.c_int32 * 11)(*[int(x) for x in list(unroll) + list(threads) + list(capped) + [l2, overlap]])
         check(lib().mpaso_state_set_launch_config(self._h, c))
 
