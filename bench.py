@@ -46,6 +46,8 @@ CONFIGS = {
                   level=6, app="sw", L=1, T=1, dt=90.0, fct=True, hmix=True, kappa=1e4, nu=1e4),
     "ocean_l7": dict(workload="sphere-level7 ocean tracers, 60 levels x 3 tracers, FCT + del2 (9.8M cell-levels)",
                      level=7, app="ocean", L=60, T=3, dt=300.0, fct=True, hmix=True, kappa=1e4, nu=0.0),
+    "ocean_l6": dict(workload="sphere-level6 ocean tracers, 60 levels x 3 tracers, FCT + del2 (2.5M cell-levels)",
+                     level=6, app="ocean", L=60, T=3, dt=450.0, fct=True, hmix=True, kappa=1e4, nu=0.0),
 }
 L2_BYTES = 129e6
 
@@ -427,7 +429,8 @@ def ensemble_arm(args):
         s = G.State(d, nlev=1, ntr=1, **opts)
         for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
             s.set(f, states[i][k])
-        s.set_launch_config(launch["unroll"], launch["threads"], launch["capped"], 0, launch["overlap"])
+        s.set_launch_config(launch["unroll"], launch["threads"], launch["capped"], 0, launch["overlap"],
+                            launch["split"])
         s.step_graph(dt, W)
         singles.append((d, s))
     torch.cuda.synchronize()

@@ -235,7 +235,7 @@ int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per
 int mpaso_state_launches_per_step(mpaso_state s, int32_t *n);
 int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
 
-/* Launch configuration of the three kernels of an RK stage, as 11 ints:
+/* Launch configuration of the kernels of an RK stage, as 12 ints:
  * config[0..2] = 1 where the kernel's stencil loop is unrolled at compile
  * time (only meaningful where the mesh's widest stencil is 10: the sphere),
  * config[3..5] = threads per block (64, 128 or 256), config[6..8] = 1 where
@@ -245,8 +245,11 @@ int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
  * 1 the FCT advection coefficients, 2 the TRiSK weights; config[10] = 1
  * when consecutive stage kernels use programmatic dependent launch (a kernel
  * is scheduled while its predecessor drains and waits for it in hardware; sw
- * app).  Results do not depend on the threads per block, the L2 choice or
- * the launch overlap; the other variants may
+ * app); config[11] = 1 for the four-launch schedule of the sw app with
+ * tracers (the tracer fluxes move from the first kernel into the edge threads
+ * of the second, the limiter into a kernel of its own).  Results do not
+ * depend on the threads per block, the L2 choice, the launch overlap or the
+ * schedule; the other variants may
  * differ in the last bits.  No counterpart in the reference (its tasks have
  * no device launch shape).  Setting it drops any captured step graph; a
  * persisting L2 reservation is per device context, so at most one state per
@@ -257,10 +260,11 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
 /* Per-mesh autotuner: for each stage kernel in turn, times every variant
  * (unrolled or not x capped or not x 64/128/256 threads) over nsteps steps
  * of size dt and keeps the fastest, then picks the L2 residency choice on
- * the whole stage and the launch overlap on uninterrupted steps.  The prognostic state is saved first and restored on
+ * the whole stage, the schedule on the whole stage and the launch overlap on
+ * uninterrupted steps.  The prognostic state is saved first and restored on
  * return, so the call leaves (h, u, tracers) unchanged; it allocates one
  * temporary copy of them.  config (may be NULL) receives the chosen
- * configuration (11 ints).  Call it outside stream capture. */
+ * configuration (12 ints).  Call it outside stream capture. */
 int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config);
 
 /* Adjoint of the sw RK4 step for (h, u).  No counterpart in the reference,

@@ -58,7 +58,11 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
 }
 
 // ------------------------------------------------------ K2: edges + cells
-template <int T, int NW, int OC>
+// SPLIT = 1 (the four-launch schedule): K1 computed only F, F Pv and Pv_e; the
+// edge threads here add the tracer fluxes (their stencil gathers overlap the
+// TRiSK arithmetic) and the cell threads leave the limiter, which needs every
+// edge's fluxes, to k_sw_limit.  Same arithmetic either way.
+template <int T, int NW, int OC, int SPLIT>
 __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   stage_prologue();
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -83,7 +87,8 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
     // - (ke2 - ke1 + g (h2 + b2 - h1 - b1)) / dc + nu (div2 - div1) / dc, with the
     // kinetic and divergence parts as one difference of kdiv = ke - nu div; the
     // geopotential stays a thickness difference, exact where h is uniform
-    const double dh = (S.h_in[i2] - S.h_in[i1]) + st.dhs[e];
+    const double h1 = S.h_in[i1], h2 = S.h_in[i2];
+    const double dh = (h2 - h1) + st.dhs[e];
     double tend = fma(-m.invDcEdge[e], fma(S.g, dh, S.bern[i2] - S.bern[i1]), q);
     if (S.visc) {  // - nu (vort_b - vort_a) / dv
       const int2 v = m.voe[e];
@@ -102,6 +107,8 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
         S.u_out[i] = S.pin_u ? up : fma(S.w_sub, tend, up);
         S.u_acc[i] = fma(S.w_acc, tend, S.u_acc[i]);
     }
+    if constexpr (SPLIT && T > 0)
+      edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, S.FG[i].x, h1 + h2, st.dvh, st.cpm2, st.kdh);
     return;
   }
   i -= nEL;
@@ -131,8 +138,22 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
     // provisional thickness (apps/ocean/tasks/solve.cc:60-97): h + dt tend_h
     const double hin = S.h_in[i];
     const double hpi = S.fct ? rcp_nr(fma(S.dt, tend_h, hin)) : 0.0;
-    cell_limiter<T, NC>(m, S, L, c, k, i, hin, hpi);
+    if constexpr (SPLIT)
+      S.hpw[i] = hpi;
+    else
+      cell_limiter<T, NC>(m, S, L, c, k, i, hin, hpi);
   }
+}
+
+// Limiter kernel of the four-launch schedule: bounds, upwind tendency and
+// R+- of every cell from the fluxes k_sw_tend<.., SPLIT = 1> wrote.
+template <int T, int NC, int OC>
+__global__ void MPASO_BOUNDS(OC) k_sw_limit(DMesh m, Stage S, int L) {
+  stage_prologue();
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nC * L) return;
+  const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+  cell_limiter<T, NC>(m, S, L, c, k, i, S.h_in[i], S.hpw[i]);
 }
 
 // Diagnostics of a state (u, h): at cells kdiv = ke - nu div, whose edge
@@ -364,7 +385,7 @@ Stage make_stage(SwState &s, int rk, double dt) {
   S.u_new = s.U[0], S.h_new = s.H[0], S.tr_new = s.TR0;
   S.pv = s.pv, S.vort = s.vort, S.bern = s.bern;
   S.FG = s.FG, S.pve = s.pve, S.A = s.A, S.LO = s.LO, S.DF = s.DF;
-  S.R2 = s.R2, S.tLO = s.tLO;
+  S.R2 = s.R2, S.tLO = s.tLO, S.hpw = s.HPW;
   return S;
 }
 
@@ -404,15 +425,22 @@ void launch_k1(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_
     launch_ex(k_sw_edge_pre<T, 0, OC>, n, b, win, s, st, m, s.st, S, s.L);
 }
 
-template <int T, int OC>
+template <int T, int OC, int SPLIT>
 void launch_k2(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   const int64_t n = ((int64_t)m.nE + m.nC) * s.L;
   const bool win = s.tune_l2 == 2;
   if (unroll)
-    launch_ex(k_sw_tend<T, 10, OC>, n, b, win, s, st, m, s.st, S, s.L);
+    launch_ex(k_sw_tend<T, 10, OC, SPLIT>, n, b, win, s, st, m, s.st, S, s.L);
   else
-    launch_ex(k_sw_tend<T, 0, OC>, n, b, win, s, st, m, s.st, S, s.L);
+    launch_ex(k_sw_tend<T, 0, OC, SPLIT>, n, b, win, s, st, m, s.st, S, s.L);
+  if constexpr (SPLIT && T > 0) {
+    const int64_t nc = (int64_t)m.nC * s.L;
+    if (unroll)
+      launch_pdl(k_sw_limit<T, 6, OC>, nc, b, s.tune_pdl, st, m, S, s.L);
+    else
+      launch_pdl(k_sw_limit<T, 0, OC>, nc, b, s.tune_pdl, st, m, S, s.L);
+  }
 }
 
 template <int T, int OC>
@@ -431,15 +459,29 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
   // 10-slot edge stencils (K1, K2 edges) and at most 6 edges per cell (K2, K3 cells)
   const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0), c6 = m.maxEoC <= 6;
   constexpr int OC1 = T <= kOccMaxT ? 1 : 0;  // no capped variants compiled beyond kOccMaxT
-  if (OC1 && s.tune_occ[0])
-    launch_k1<T, OC1>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
-  else
-    launch_k1<T, 0>(s, S, w10 && s.tune_unroll[0], s.tune_tpb[0], st);
+  const bool split = T > 0 && s.tune_split;    // four-launch schedule
+  const bool u1 = w10 && s.tune_unroll[0], u2 = w10 && c6 && s.tune_unroll[1];
+  if (split) {  // K1 does the thickness flux part only (the T = 0 kernel)
+    if (s.tune_occ[0])
+      launch_k1<0, 1>(s, S, u1, s.tune_tpb[0], st);
+    else
+      launch_k1<0, 0>(s, S, u1, s.tune_tpb[0], st);
+  } else if (OC1 && s.tune_occ[0]) {
+    launch_k1<T, OC1>(s, S, u1, s.tune_tpb[0], st);
+  } else {
+    launch_k1<T, 0>(s, S, u1, s.tune_tpb[0], st);
+  }
   if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
-  if (OC1 && s.tune_occ[1])
-    launch_k2<T, OC1>(s, S, w10 && c6 && s.tune_unroll[1], s.tune_tpb[1], st);
-  else
-    launch_k2<T, 0>(s, S, w10 && c6 && s.tune_unroll[1], s.tune_tpb[1], st);
+  if (split) {
+    if (OC1 && s.tune_occ[1])
+      launch_k2<T, OC1, 1>(s, S, u2, s.tune_tpb[1], st);
+    else
+      launch_k2<T, 0, 1>(s, S, u2, s.tune_tpb[1], st);
+  } else if (OC1 && s.tune_occ[1]) {
+    launch_k2<T, OC1, 0>(s, S, u2, s.tune_tpb[1], st);
+  } else {
+    launch_k2<T, 0, 0>(s, S, u2, s.tune_tpb[1], st);
+  }
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
   if (OC1 && s.tune_occ[2])
     launch_k3<T, OC1>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
@@ -498,7 +540,8 @@ void sw_create(SwState &s) {
       {&s.TR0, nC * L * T}, {&s.TRA, nC * L * T}, {&s.TRB, nC * L * T}, {&s.TRH, nC * L * T},
       {&s.pv, nV * L}, {&s.vort, nV * L}, {&s.bern, nC * L},
       {(double **)&s.FG, 2 * nE * L}, {&s.pve, nE * L}, {&s.A, nE * L * T}, {&s.LO, nE * L * T},
-      {&s.DF, nE * L * T}, {(double **)&s.R2, 2 * nC * L * T}, {&s.tLO, nC * L * T}};
+      {&s.DF, nE * L * T}, {(double **)&s.R2, 2 * nC * L * T}, {&s.tLO, nC * L * T},
+      {&s.HPW, T > 0 ? nC * L : 0}};
   stat_buffers(s, bufs);
   alloc_arena(s, bufs);
   build_stat(s);
@@ -690,6 +733,7 @@ void get_config(const SwState &S, int32_t *config) {
     config[k] = S.tune_unroll[k], config[3 + k] = S.tune_tpb[k], config[6 + k] = S.tune_occ[k];
   config[9] = S.tune_l2;
   config[10] = S.tune_pdl;
+  config[11] = S.tune_split;
 }
 
 constexpr int kTpbChoices[3] = {64, 128, 256};
@@ -962,6 +1006,7 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
     }
     require(config[9] >= 0 && config[9] <= 2, MPASO_ERR_ARG, "L2 window choice must be 0, 1 or 2");
     require(config[10] == 0 || config[10] == 1, MPASO_ERR_ARG, "launch overlap flag must be 0 or 1");
+    require(config[11] == 0 || config[11] == 1, MPASO_ERR_ARG, "schedule flag must be 0 or 1");
     SwState &S = s->s;
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
@@ -970,6 +1015,7 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
       S.tune_unroll[k] = config[k], S.tune_tpb[k] = config[3 + k], S.tune_occ[k] = config[6 + k];
     set_l2_window(S, config[9]);
     S.tune_pdl = config[10];
+    S.tune_split = S.p.app == MPASO_APP_SW && S.T > 0 ? config[11] : 0;
   });
 }
 
@@ -1034,6 +1080,19 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
         if (tot < 0.98 * best) best = tot, best_l2 = w;  // keep the simpler choice unless clearly faster
       }
       set_l2_window(S, best_l2);
+      // four-launch schedule (sw with tracers), judged on the whole stage
+      if (S.p.app == MPASO_APP_SW && S.T > 0) {
+        double tot[2];
+        for (int sp = 0; sp <= 1; ++sp) {
+          S.tune_split = sp;
+          save_restore(false);
+          time_stage_kernels(S, dt, 1, ms);
+          save_restore(false);
+          time_stage_kernels(S, dt, nsteps, ms);
+          tot[sp] = ms[0] + ms[1] + ms[2];
+        }
+        S.tune_split = tot[1] < 0.98 * tot[0] ? 1 : 0;
+      }
       // programmatic dependent launch (sw stage kernels), judged on uninterrupted steps
       if (S.p.app == MPASO_APP_SW) {
         double t[2];

@@ -94,6 +94,7 @@ struct Stage {
   double *tLO;                              // cell intermediates
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
   double *tape_pv, *tape_hs;                // adjoint taping: pv and kite-summed h of the next state
+  double *hpw;                              // sw four-launch schedule: 1/hProv from K2 to the limiter
 };
 
 // State context (sw or ocean app).
@@ -136,6 +137,10 @@ struct SwState {
   // stage kernels launched with programmatic dependent launch (sw app; off
   // unless the autotuner measures it faster)
   int tune_pdl = 0;
+  // sw with tracers: four launches per stage (tracer fluxes in K2's edge
+  // threads, limiter in its own kernel) instead of three
+  int tune_split = 0;
+  double *HPW = nullptr;
   ~SwState();
 };
 

@@ -282,24 +282,27 @@ class State:
     @staticmethod
     def _cfg_dict(c):
         return {"unroll": [int(x) for x in c[:3]], "threads": [int(x) for x in c[3:6]],
-                "capped": [int(x) for x in c[6:9]], "l2": int(c[9]), "overlap": int(c[10])}
+                "capped": [int(x) for x in c[6:9]], "l2": int(c[9]), "overlap": int(c[10]),
+                "split": int(c[11])}
 
     def launch_config(self):
         """{'unroll', 'threads', 'capped'}: one value per stage kernel; 'l2': the
         static array kept resident in L2 (0 none, 1 advection coefficients, 2 TRiSK weights);
-        'overlap': programmatic dependent launch between stage kernels."""
-        c = (ctypes.c_int32 * 11)()
+        'overlap': programmatic dependent launch between stage kernels; 'split': the
+        four-launch schedule (sw with tracers)."""
+        c = (ctypes.c_int32 * 12)()
         check(lib().mpaso_state_launch_config(self._h, c))
         return self._cfg_dict(c)
 
-    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=0):
-        c = (ctypes.c_int32 * 11)(*[int(x) for x in list(unroll) + list(threads) + list(capped) + [l2, overlap]])
+    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=0, split=0):
+        c = (ctypes.c_int32 * 12)(*[int(x) for x in list(unroll) + list(threads) + list(capped) +
+                                    [l2, overlap, split]])
         check(lib().mpaso_state_set_launch_config(self._h, c))
 
     def autotune(self, dt, nsteps=3):
         """Times every launch variant of each stage kernel on this mesh and keeps
         the fastest; (h, u, tracers) are restored afterwards.  Returns the choice."""
-        c = (ctypes.c_int32 * 11)()
+        c = (ctypes.c_int32 * 12)()
         check(lib().mpaso_state_autotune(self._h, ctypes.c_double(dt), int(nsteps), c))
         return self._cfg_dict(c)
 

@@ -15,8 +15,9 @@ from test_gpu_rk4 import make_state
 pytestmark = pytest.mark.gpu
 TOL1 = 1e-12
 
-CONFIGS = [([1, 1, 1], [256, 256, 256], [0, 0, 0], 0, 1), ([0, 0, 0], [256, 256, 256], [1, 1, 1], 1, 0),
-           ([1, 1, 1], [64, 128, 64], [1, 0, 1], 2, 1), ([0, 1, 0], [128, 64, 256], [0, 1, 0], 1, 0)]
+CONFIGS = [([1, 1, 1], [256, 256, 256], [0, 0, 0], 0, 1, 0), ([0, 0, 0], [256, 256, 256], [1, 1, 1], 1, 0, 1),
+           ([1, 1, 1], [64, 128, 64], [1, 0, 1], 2, 1, 1), ([0, 1, 0], [128, 64, 256], [0, 1, 0], 1, 0, 0),
+           ([1, 1, 1], [128, 128, 128], [0, 0, 0], 0, 0, 1)]
 
 
 def _fields(st, app):
@@ -38,6 +39,7 @@ def test_every_launch_variant_matches_goldens(name, cfg):
         "unroll": CONFIGS[cfg][0], "threads": CONFIGS[cfg][1], "capped": CONFIGS[cfg][2]}
     assert got_cfg["l2"] in (0, CONFIGS[cfg][3])  # 0 where the state has no such array
     assert got_cfg["overlap"] == CONFIGS[cfg][4]
+    assert got_cfg["split"] == (CONFIGS[cfg][5] if g.app == "sw" and g.T > 0 else 0)
     st.step_graph(g.dt, 1)
     got = _fields(st, g.app)
     want = [g["tr_1"]] + ([g["h_1"], g["u_1"]] if g.app == "sw" else [])
@@ -71,6 +73,7 @@ def test_autotune_restores_state_and_keeps_parity(name):
     cfg = st.autotune(g.dt, 2)
     assert all(b in (64, 128, 256) for b in cfg["threads"]) and all(u in (0, 1) for u in cfg["unroll"])
     assert all(o in (0, 1) for o in cfg["capped"]) and cfg["l2"] in (0, 1, 2) and cfg["overlap"] in (0, 1)
+    assert cfg["split"] in (0, 1)
     assert st.launch_config() == cfg
     for a, b in zip(_fields(st, g.app), before):
         assert np.array_equal(a, b)
