@@ -198,14 +198,17 @@ def gpu_arm(args, cfg):
                 else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": int(kb),
                 "kernel_time_share": round(prof[top] / prof_total, 3)}
-    fp64 = {"achieved_dfma_per_s": kf / (prof[top] * 1e-3), "peak_dfma_per_s": fp64_peak,
-            "frac": round(kf / (prof[top] * 1e-3) / fp64_peak, 4), "kernel": top,
-            "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / fp64_peak, 4),
-            "nominal_dfma_per_s": 2.0 * torch.cuda.get_device_properties(local).multi_processor_count
-                                  * (clocks.get("sm_max_mhz") or 2070.0) * 1e6,
-            "note": "FP64 instructions per launch from mpaso/perfmodel.py / measured launch time, "
-                    "against the live DFMA issue rate of mpaso_probe_fp64 (independent DFMA chains; "
-                    "the nominal 2 DFMA/clk/SM is not reached by any instruction mix measured)"}
+    # FP64 pipe peak: 2 DFMA/DADD/DMUL per clock per SM (ncu's peak for the pipe; the
+    # ocean edge kernel sustains 91% of it).  A chain of dependent DFMAs alone (the
+    # probe) issues at ~0.80 of it.
+    pipe_peak = 2.0 * torch.cuda.get_device_properties(local).multi_processor_count * \
+        (clocks.get("sm_max_mhz") or 2070.0) * 1e6
+    fp64 = {"achieved_per_s": kf / (prof[top] * 1e-3), "peak_per_s": pipe_peak,
+            "frac": round(kf / (prof[top] * 1e-3) / pipe_peak, 4), "kernel": top,
+            "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / pipe_peak, 4),
+            "dfma_chain_probe_per_s": fp64_peak,
+            "note": "FP64 instructions per launch from mpaso/perfmodel.py (within ~10% of ncu's counts) "
+                    "/ measured launch time, against the FP64 pipe peak of 2 per clock per SM"}
     step_hbm = {"algorithmic_bytes_per_step": int(step_bytes),
                 "achieved_gbs": round(step_bytes / (ms_max * 1e-3 / K) / 1e9, 1),
                 "frac": round(step_bytes / (ms_max * 1e-3 / K) / 1e9 / peak, 4),
