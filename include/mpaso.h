@@ -224,6 +224,17 @@ int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps);
 int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
                         double *tracers);
 int mpaso_state_sync(mpaso_state s);
+/* History output without stalling the time loop (the reference writes history
+ * synchronously, mpasoflecsi/tasks/io.cc:160-254): enqueues a copy of `field`
+ * as it stands after the work already queued on the state's stream into
+ * host memory `data` (reference numbering) and returns at once.  A side
+ * stream permutes the field into one of two device buffers used in turn and
+ * copies it out; later steps wait only for the permutation, not for the copy.
+ * `data` should be page-locked for the copy to be asynchronous, and must not
+ * be read before mpaso_state_snapshot_wait returns.  No counterpart in the
+ * reference's task interface. */
+int mpaso_state_snapshot(mpaso_state s, int32_t field, double *data);
+int mpaso_state_snapshot_wait(mpaso_state s);
 int mpaso_state_stream(mpaso_state s, void **stream);
 /* Per-kernel timing: runs nsteps steps (not from a graph) with CUDA events
  * around every launch on the state's stream and returns, for each of the

@@ -135,14 +135,20 @@ void ocean_create(SwState &s) {
   build_stat(s);
 }
 
+void ocean_recompute(SwState &s, double dt, cudaStream_t st);
+
 void ocean_prepare(SwState &s, double dt, cudaStream_t st) {
+  if (s.prep_dt != dt) ocean_recompute(s, dt, st);
+}
+
+// Thickness flux and 1/hProv of the stored (h, u), unconditionally (also from
+// inside a stream capture, after new h / u were gathered in).
+void ocean_recompute(SwState &s, double dt, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
-  if (s.prep_dt != dt) {
-    k_oc_prep<<<blocks_for(((int64_t)m.nE + m.nC) * s.L, TPB), TPB, 0, st>>>(m, s.st, s.L, s.U[0], s.H[0],
-                                                                          s.HE, s.F, s.HPI, dt);
-    MPASO_CUDA(cudaGetLastError());
-    s.prep_dt = dt;
-  }
+  k_oc_prep<<<blocks_for(((int64_t)m.nE + m.nC) * s.L, TPB), TPB, 0, st>>>(m, s.st, s.L, s.U[0], s.H[0],
+                                                                        s.HE, s.F, s.HPI, dt);
+  MPASO_CUDA(cudaGetLastError());
+  s.prep_dt = dt;
 }
 
 void ocean_one_stage(SwState &s, int rk, double dt, cudaStream_t st) {

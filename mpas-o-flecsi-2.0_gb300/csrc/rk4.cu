@@ -313,6 +313,15 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
 // ------------------------------------------------------------ state context
 SwState::~SwState() {
   if (graph) cudaGraphExecDestroy(graph);
+  if (xg) cudaGraphExecDestroy(xg);
+  if (out_stream) cudaStreamSynchronize(out_stream);
+  for (int b = 0; b < 2; ++b) {
+    if (out_buf[b]) cudaFree(out_buf[b]);
+    if (out_read[b]) cudaEventDestroy(out_read[b]);
+    if (out_done[b]) cudaEventDestroy(out_done[b]);
+  }
+  if (out_ready) cudaEventDestroy(out_ready);
+  if (out_stream) cudaStreamDestroy(out_stream);
   if (io_stage) cudaFree(io_stage);
   if (tune_l2) {  // hand the persisting L2 lines back
     cudaCtxResetPersistingL2Cache();
@@ -527,6 +536,7 @@ void sw_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
 void ocean_create(SwState &s);
 void ocean_steps(SwState &s, double dt, int nsteps, cudaStream_t st);
 void ocean_prepare(SwState &s, double dt, cudaStream_t st);
+void ocean_recompute(SwState &s, double dt, cudaStream_t st);
 void ocean_one_stage(SwState &s, int rk, double dt, cudaStream_t st);
 int ocean_launches_per_step(const SwState &s);
 
@@ -674,6 +684,10 @@ void drop_graph(SwState &S) {
   if (S.graph) {
     MPASO_CUDA(cudaGraphExecDestroy(S.graph));
     S.graph = nullptr;
+  }
+  if (S.xg) {
+    MPASO_CUDA(cudaGraphExecDestroy(S.xg));
+    S.xg = nullptr;
   }
   drop_adjoint_graph(S);
 }
@@ -832,6 +846,62 @@ int mpaso_state_set(mpaso_state s, int32_t field, const double *data) {
   });
 }
 
+int mpaso_state_snapshot(mpaso_state s, int32_t field, double *data) {
+  return guarded("mpaso_state_snapshot", [&] {
+    require(s && data, MPASO_ERR_ARG, "null argument");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    int entity;
+    int64_t row;
+    double *buf;
+    field_geom(S, field, entity, row, buf);
+    MeshCtx &ctx = S.mesh->ctx;
+    const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : entity == MPASO_EDGES ? ctx.d.nE : ctx.d.nV;
+    const size_t bytes = (size_t)n * row * sizeof(double);
+    if (!S.out_stream) {
+      MPASO_CUDA(cudaStreamCreateWithFlags(&S.out_stream, cudaStreamNonBlocking));
+      MPASO_CUDA(cudaEventCreateWithFlags(&S.out_ready, cudaEventDisableTiming));
+      for (int b = 0; b < 2; ++b) {
+        MPASO_CUDA(cudaEventCreateWithFlags(&S.out_read[b], cudaEventDisableTiming));
+        MPASO_CUDA(cudaEventCreateWithFlags(&S.out_done[b], cudaEventDisableTiming));
+      }
+    }
+    if (S.out_bytes < bytes) {  // (re)size both buffers once every earlier copy has ended
+      MPASO_CUDA(cudaStreamSynchronize(S.out_stream));
+      for (auto &p : S.out_buf) {
+        if (p) MPASO_CUDA(cudaFree(p));
+        p = nullptr;
+      }
+      S.out_bytes = 0;
+      for (auto &p : S.out_buf)
+        if (cudaMalloc((void **)&p, bytes) != cudaSuccess) {
+          cudaGetLastError();
+          fail(MPASO_ERR_ALLOC, "device allocation of the snapshot buffers failed");
+        }
+      S.out_bytes = bytes;
+    }
+    const int b = S.out_next;
+    S.out_next ^= 1;
+    // the field as it stands after the work already queued on the state's stream
+    MPASO_CUDA(cudaEventRecord(S.out_ready, S.stream));
+    MPASO_CUDA(cudaStreamWaitEvent(S.out_stream, S.out_ready, 0));
+    // the buffer's previous copy to the host must be over before it is refilled
+    k_scatter_rows_pub(buf, S.out_buf[b], ctx.d_perm[entity], n, (int)row, S.out_stream);
+    MPASO_CUDA(cudaEventRecord(S.out_read[b], S.out_stream));
+    // later steps may overwrite the field only once the permutation has read it
+    MPASO_CUDA(cudaStreamWaitEvent(S.stream, S.out_read[b], 0));
+    MPASO_CUDA(cudaMemcpyAsync(data, S.out_buf[b], bytes, cudaMemcpyDeviceToHost, S.out_stream));
+    MPASO_CUDA(cudaEventRecord(S.out_done[b], S.out_stream));
+  });
+}
+
+int mpaso_state_snapshot_wait(mpaso_state s) {
+  return guarded("mpaso_state_snapshot_wait", [&] {
+    require(s != nullptr, MPASO_ERR_ARG, "null state");
+    if (s->s.out_stream) MPASO_CUDA(cudaStreamSynchronize(s->s.out_stream));
+  });
+}
+
 int mpaso_state_get(mpaso_state s, int32_t field, double *data) {
   return guarded("mpaso_state_get", [&] {
     require(s && data, MPASO_ERR_ARG, "null argument");
@@ -880,25 +950,73 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
     const cudaStream_t st = S.stream;
     const size_t bytes = (size_t)(nh + nu + nt) * sizeof(double);
     double *dh = ensure_io(S, bytes), *du = dh + nh, *dtr = du + nu;
+    // Page-locked buffers: the whole exchange (copies in, permutations, steps,
+    // copies out) is one graph, captured once per buffer set, dt and nsteps.
+    bool locked = true;
+    for (const void *p : {(const void *)h, (const void *)u, (const void *)(tr ? tracers : h)}) {
+      cudaPointerAttributes a;
+      if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) locked = false;
+      cudaGetLastError();
+    }
+    const XKey key{h, u, tr ? tracers : nullptr, dt, nsteps};
+    if (locked && S.xg && S.xkey == key) {
+      MPASO_CUDA(cudaGraphLaunch(S.xg, st));
+      MPASO_CUDA(cudaStreamSynchronize(st));
+      return;
+    }
+    if (S.xg) {
+      MPASO_CUDA(cudaGraphExecDestroy(S.xg));
+      S.xg = nullptr;
+    }
+    if (locked) MPASO_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     // one copy per field each way (copy engines; page-locked buffers go at link speed),
     // the permutations on the device, one synchronisation.  (Letting the permutation
     // kernels read and write mapped host memory directly was slower: their accesses
     // are scattered.)
+    try {
     MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
     MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, st));
     if (tr) MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, st));
     k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
     k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
     if (tr) k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
-    S.diag_valid = false;
-    S.prep_dt = 0.0;
-    step_graph(S, dt, nsteps);
+    if (locked) {  // inside the capture: the steps' kernels themselves
+      if (S.p.app == MPASO_APP_SW) {
+        S.diag_valid = false;
+        ensure_diag(S, st);
+      } else {
+        ocean_recompute(S, dt, st);
+      }
+      run_steps(S, dt, nsteps, st);
+    } else {
+      S.diag_valid = false;
+      S.prep_dt = 0.0;
+      step_graph(S, dt, nsteps);
+    }
     k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
     k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
     if (tr) k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
     MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, st));
     MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (tr) MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    } catch (...) {
+      if (locked) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+      }
+      throw;
+    }
+    if (locked) {
+      cudaGraph_t g;
+      MPASO_CUDA(cudaStreamEndCapture(st, &g));
+      const cudaError_t e = cudaGraphInstantiate(&S.xg, g, 0);
+      cudaGraphDestroy(g);
+      MPASO_CUDA(e);
+      S.xkey = key;
+      MPASO_CUDA(cudaGraphLaunch(S.xg, st));
+    }
     MPASO_CUDA(cudaStreamSynchronize(st));
   });
 }

@@ -97,6 +97,16 @@ struct Stage {
   double *hpw;                              // sw four-launch schedule: 1/hProv from K2 to the limiter
 };
 
+// Buffers and step parameters a captured host-exchange graph was built for.
+struct XKey {
+  const void *h = nullptr, *u = nullptr, *tr = nullptr;
+  double dt = 0.0;
+  int nsteps = -1;
+  bool operator==(const XKey &o) const {
+    return h == o.h && u == o.u && tr == o.tr && dt == o.dt && nsteps == o.nsteps;
+  }
+};
+
 // State context (sw or ocean app).
 struct SwState {
   mpaso_mesh mesh = nullptr;
@@ -119,6 +129,16 @@ struct SwState {
   // device staging of mpaso_rk4_step_host (reference-ordered h, u, tracers)
   double *io_stage = nullptr;
   size_t io_bytes = 0;
+  // mpaso_rk4_step_host with page-locked buffers: the captured exchange graph
+  cudaGraphExec_t xg = nullptr;
+  XKey xkey{};
+  // history output (mpaso_state_snapshot): side stream, two staging buffers
+  // used in turn, events ordering them against the stepping stream
+  cudaStream_t out_stream = nullptr;
+  double *out_buf[2] = {nullptr, nullptr};
+  size_t out_bytes = 0;
+  int out_next = 0;
+  cudaEvent_t out_ready = nullptr, out_read[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
   // optional per-launch timing: events recorded after every kernel of a stage
   cudaEvent_t *prof_events = nullptr;
   // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu

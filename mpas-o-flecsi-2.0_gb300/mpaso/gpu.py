@@ -264,6 +264,15 @@ class State:
     def sync(self):
         check(lib().mpaso_state_sync(self._h))
 
+    def snapshot(self, field, out):
+        """Asynchronous copy of a field into `out` (page-locked for overlap); valid after
+        snapshot_wait()."""
+        check(lib().mpaso_state_snapshot(self._h, int(field), _ptr(out)))
+        return out
+
+    def snapshot_wait(self):
+        check(lib().mpaso_state_snapshot_wait(self._h))
+
     def stream(self):
         s = ctypes.c_void_p()
         check(lib().mpaso_state_stream(self._h, ctypes.byref(s)))

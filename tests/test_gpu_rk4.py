@@ -178,3 +178,24 @@ def test_host_boundary_call_with_page_locked_buffers():
     hp, up, tp = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (g["h0"], g["u0"], g["tr0"]))
     st2.step_host(g.dt, 2, hp, up, tp)
     assert np.array_equal(hp.numpy(), h) and np.array_equal(up.numpy(), u) and np.array_equal(tp.numpy(), tr)
+
+
+def test_history_snapshots_while_stepping():
+    """Snapshots taken between graph-replayed steps, copied out asynchronously while
+    later steps run, equal the state read synchronously at the same points."""
+    torch = pytest.importorskip("torch")
+    import mpaso.gpu as G
+    g = Golden("sw_fct_icosa3_L1T1")
+    _, st = make_state(g)
+    _, ref = make_state(g)
+    snaps, want = [], []
+    for n in range(4):
+        st.step_graph(g.dt, 2)
+        hp = torch.empty(g["h0"].shape, dtype=torch.float64).pin_memory()
+        tp = torch.empty(g["tr0"].shape, dtype=torch.float64).pin_memory()
+        snaps.append((st.snapshot(G.FIELD_H, hp), st.snapshot(G.FIELD_TRACERS, tp)))
+        ref.step_graph(g.dt, 2)
+        want.append((ref.get(G.FIELD_H), ref.get(G.FIELD_TRACERS)))
+    st.snapshot_wait()
+    for (hp, tp), (h, tr) in zip(snaps, want):
+        assert np.array_equal(hp.numpy(), h) and np.array_equal(tp.numpy(), tr)
