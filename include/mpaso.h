@@ -224,8 +224,9 @@ int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps);
 int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
                         double *tracers);
 int mpaso_state_sync(mpaso_state s);
-/* History output without stalling the time loop (the reference writes history
- * synchronously, mpasoflecsi/tasks/io.cc:160-254): enqueues a copy of `field`
+/* History output without stalling the time loop (the reference writes each
+ * output step synchronously: the field_output_wrapper task of apps/sw/run.cc:10
+ * via write_timestep, mpasoflecsi/io/helpers.hh:127-151): enqueues a copy of `field`
  * as it stands after the work already queued on the state's stream into
  * host memory `data` (reference numbering) and returns at once.  A side
  * stream permutes the field into one of two device buffers used in turn and
