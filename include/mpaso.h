@@ -279,23 +279,38 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
  * configuration (12 ints).  Call it outside stream capture. */
 int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config);
 
-/* Adjoint of the sw RK4 step for (h, u).  No counterpart in the reference,
- * which has no adjoint: these differentiate what mpaso_rk4_step computes for
- * app = MPASO_APP_SW (apps/sw/run.cc:10-60) with fct = hmix = 0 semantics
- * for the tracers (passive) and pin_u = 0.
+/* Adjoint of the sw RK4 step.  No counterpart in the reference, which has no
+ * adjoint: these differentiate what mpaso_rk4_step computes for app =
+ * MPASO_APP_SW (apps/sw/run.cc:10-60) with pin_u = 0.
  *
  * mpaso_rk4_forward: advances the state nsteps steps of size dt like
- * mpaso_rk4_step, keeping a checkpoint of (h, u) every ckpt_every steps.
+ * mpaso_rk4_step, keeping a checkpoint of (h, u, tracers) every ckpt_every
+ * steps.
  * mpaso_rk4_vjp: given the cotangents gh (nCells x nlev) and gu (nEdges x
  * nlev) of the state after the forward run, writes dJ/dh0 and dJ/du0 of the
  * state before it into gh0 / gu0 (reference ordering; host or device
- * pointers).  Stage states are recomputed segment by segment from the
- * checkpoints.  Device memory: ceil(N / ckpt_every) + 4 ckpt_every + 2
- * copies of (h, u), 4 ckpt_every + 1 copies of two vertex fields (the taped
- * pv and kite-summed thickness), and about 20 work arrays of one level-field
- * each. */
+ * pointers).  (h, u) do not depend on the tracers, so this reverse leaves
+ * them out.  Stage states are recomputed segment by segment from the
+ * checkpoints.
+ * mpaso_rk4_vjp_tracers: the same with the tracers: gtr / gtr0 are the
+ * cotangents of the final / initial tracer concentrations (nCells x nlev x
+ * ntr), and gh0 includes what h contributes through the tracer transport.
+ * With fct = 1 the FCT limiter (apps/ocean/tasks/solve.cc:169-326) is
+ * differentiated on the branch its forward evaluation takes (each max, min,
+ * clamp and sign as evaluated, ties to the reference's first argument);
+ * hmix del2 mixing and the centred flux of fct = 0 are linear in the
+ * tracers.
+ * Device memory: ceil(N / ckpt_every) + 4 ckpt_every + 2 copies of (h, u),
+ * 4 ckpt_every + 1 copies of two vertex fields (the taped pv and
+ * kite-summed thickness), and about 20 work arrays of one level-field each;
+ * with tracers also ceil(N / ckpt_every) + 4 ckpt_every + 1 copies of the
+ * tracers, 4 ckpt_every copies of two edge-tracer fields (fluxes A, LO) and
+ * of the two limiter factors, and about 15 work arrays of one level-tracer
+ * field. */
 int mpaso_rk4_forward(mpaso_state s, double dt, int32_t nsteps, int32_t ckpt_every);
 int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0, double *gu0);
+int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, const double *gtr,
+                          double *gh0, double *gu0, double *gtr0);
 int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);
 
 /* FP64 ceiling of `device`: DFMA lane-operations per second issued by a

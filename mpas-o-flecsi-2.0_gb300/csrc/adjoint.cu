@@ -1,5 +1,6 @@
 // Hand-written adjoint (vector-Jacobian product) of the fused sw RK4 step for
-// (h, u), with uniform checkpointing.
+// (h, u) and, optionally, the tracers (FCT advection + del2 mixing), with
+// uniform checkpointing.
 //
 // Forward per stage (rk4.cu), in the quantities the adjoint needs:
 //   circ_v = sum sdc u,  hs_v = sum kite h,  pv_v = (f A + circ) / hs
@@ -26,6 +27,21 @@
 // with J_s the Jacobian of the tendency at stage state s.  Stage states are
 // recomputed segment by segment from checkpoints kept every `ckpt_every`
 // steps and taped for the segment being reversed.
+//
+// Tracers.  The sw step is linear-RK in (u, h, q = h tr) (apps/sw/tasks/
+// solve.cc:162, 300-302, 337, 354): stage inputs tr_s = q_s / h_s, the
+// tracer tendency Tq(u_s, h_s, tr_s) feeds q like tend_h feeds h.  So the
+// same RK recursion runs on (lam_q, acc_q, lk_q), and a stage adds
+//   mu_q = (dTq/dtr)^T lk_q / h_s,
+//   mu_h += (dTq/dh)^T lk_q - sum_t (dTq/dtr)^T lk_q tr_s / h_s,
+//   mu_u += (dTq/du)^T lk_q,
+// with (q, h) <-> (tr, h) converted only at the ends of the window.  The FCT
+// limiter (apps/ocean/tasks/solve.cc:169-326) is differentiated on the branch
+// its forward evaluation takes: every max / min / clamp / sign picks the
+// argument the forward picked (ties as the reference's max / min: the first
+// argument), and the derivative flows through that argument only.  The
+// stage's fluxes A, LO and limiter factors R+/R- are taped by the recompute;
+// bounds, provisional thickness and upwind values are recomputed.
 #include <cstring>
 
 #include "rk4.cuh"
@@ -47,10 +63,23 @@ struct AdjBuffers {
   double *lam_u = nullptr, *lam_h = nullptr, *acc_u = nullptr, *acc_h = nullptr;
   double *lk_u = nullptr, *lk_h = nullptr, *mu_u = nullptr, *mu_h = nullptr;
   double *lhe = nullptr, *lpve = nullptr, *lke = nullptr, *ldiv = nullptr, *lcirc = nullptr, *lhs = nullptr;
-  // the whole reverse sweep, captured once per (N, k, dt) and replayed
+  // tracers (allocated when the state has any): checkpoints and stage tape of
+  // the concentrations, the stage fluxes and limiter factors, cotangents of
+  // q = h tr, and the limiter adjoint's per-cell / per-edge intermediates
+  double *ck_tr = nullptr, *tp_tr = nullptr;  // [nck][nC L T], [4k + 1][nC L T]
+  double *tp_A = nullptr, *tp_LO = nullptr;   // [4k][nE L T]
+  double2 *tp_R2 = nullptr;                   // [4k][nC L T] {R+, R-}
+  double *trhacc = nullptr;
+  double *lam_q = nullptr, *acc_q = nullptr, *lk_q = nullptr;
+  double *ltl = nullptr, *lfi = nullptr, *lfo = nullptr, *lmx = nullptr, *lmn = nullptr, *ltrs = nullptr;
+  int *amx = nullptr, *amn = nullptr;
+  double *muh_t = nullptr, *lFt = nullptr, *lhet = nullptr, *Ft = nullptr, *lhof = nullptr;
+  double2 *p12 = nullptr;
+  // the whole reverse sweep, captured once per (N, k, dt, tracers) and replayed
   cudaGraphExec_t rev = nullptr;
-  int rev_N = 0, rev_k = 0;
+  int rev_N = 0, rev_k = 0, rev_tr = 0;
   double rev_dt = 0.0;
+  int tr = 0;  // the sweep being run reverses the tracers too
 };
 
 void drop_adjoint_graph(SwState &s) {
@@ -84,8 +113,25 @@ struct AdjArgs {
   double *mu_u, *mu_h;                        // J^T lk
   double *lhe, *lpve, *lke, *ldiv, *lcirc, *lhs;
   double *lam_u, *lam_h, *acc_u, *acc_h;
+  const double *lFt, *lhet, *muh_t;           // tracer terms (null without tracers)
   int rk, visc;
   double dt, g, nu;
+};
+
+// Tracer part of one stage's reverse (see the header).
+struct TrArgs {
+  const double *u, *h, *tr;        // stage input (tape)
+  const double *A, *LO;            // stage fluxes (tape)
+  const double2 *R2;               // stage limiter factors (tape)
+  const double *kd;                // del2 coefficient per edge
+  double *lk_h;                    // thickness-tendency cotangent, + dt lambda_hProv in place
+  double *lk_q, *lam_q, *acc_q;
+  double *ltl, *lfi, *lfo, *lmx, *lmn, *ltrs;
+  int *amx, *amn;
+  double *muh_t, *lFt, *lhet, *Ft, *lhof;
+  double2 *p12;
+  int T, rk, fct, hmix;
+  double dt;
 };
 
 // Edge quantities of a stage state that B1 gathers: F = u he, pve from the taped
@@ -135,10 +181,16 @@ __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
   const double he = 0.5 * (a.h[i1] + a.h[i2]);
   const double Fe = a.FP[i].x, pve = a.pve[i], ue = a.u[i];
   const double dth = a.lk_h[i2] * m.invAreaCell[c.y] - a.lk_h[i1] * m.invAreaCell[c.x];
-  const double lF = fma(0.5, fma(pve, t1, t2), m.dvEdge[e] * dth);
+  double lF = fma(0.5, fma(pve, t1, t2), m.dvEdge[e] * dth);
   a.lpve[i] = 0.5 * fma(a.lk_u[i], s1, Fe * t1);
-  a.mu_u[i] = lF * he;
-  a.lhe[i] = lF * ue;
+  if (a.lFt) {
+    lF += a.lFt[i];
+    a.mu_u[i] = lF * he;
+    a.lhe[i] = fma(lF, ue, a.lhet[i]);
+  } else {
+    a.mu_u[i] = lF * he;
+    a.lhe[i] = lF * ue;
+  }
 }
 
 // B2 (cells + vertices): gradient terms, h_e -> h, pv -> (circ, hs).
@@ -160,7 +212,7 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
       for_slots<6>(m.nEoC[c], slot);
     else
       for_slots<0>(m.nEoC[c], slot);
-    a.mu_h[i] = fma(0.5, sl, -a.g * G);
+    a.mu_h[i] = fma(0.5, sl, -a.g * G) + (a.muh_t ? a.muh_t[i] : 0.0);
     a.lke[i] = -G;
     if (a.visc) a.ldiv[i] = a.nu * G;
     return;
@@ -186,11 +238,10 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
 }
 
 // RK4 cotangent bookkeeping for one element once mu is complete.
-__device__ __forceinline__ double combine(const AdjArgs &a, int64_t i, double mu, double *lam, double *acc,
+__device__ __forceinline__ double combine(int rk, double dt, int64_t i, double mu, double *lam, double *acc,
                                           double *lk) {
-  const double dt = a.dt;
   double l;
-  switch (a.rk) {
+  switch (rk) {
     case 3:
       acc[i] = lam[i] + mu;
       l = fma(dt, mu, (dt / 3) * lam[i]);
@@ -226,7 +277,7 @@ __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, in
       const int64_t s = (int64_t)j * m.nC + c;
       mh = fma(m.kiteR[s], a.lhs[(int64_t)m.vocR[s] * L + k], mh);
     }
-    combine(a, i, mh, a.lam_h, a.acc_h, a.lk_h);
+    combine(a.rk, a.dt, i, mh, a.lam_h, a.acc_h, a.lk_h);
     return;
   }
   i -= nCL;
@@ -240,9 +291,257 @@ __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, in
   mu = fma(m.dcEdge[e], a.lcirc[(int64_t)v.y * L + k] - a.lcirc[(int64_t)v.x * L + k], mu);
   mu = fma(2.0 * a.u[i] * st.kw[e], fma(a.lke[i1], ia1, a.lke[i2] * ia2), mu);
   if (a.visc) mu = fma(-m.dvEdge[e], fma(a.ldiv[i2], ia2, -a.ldiv[i1] * ia1), mu);
-  const double lk = combine(a, i, mu, a.lam_u, a.acc_u, a.lk_u);
+  const double lk = combine(a.rk, a.dt, i, mu, a.lam_u, a.acc_u, a.lk_u);
   // the next stage's B1 inputs (B1 of this stage has completed)
   if (a.prep) prep_edge(m, a, L, e, k, i, a.un, a.hn, a.pvn, lk);
+}
+
+// ---------------------------------------------------------------------------
+// Tracer reverse, three launches per stage ahead of B1: TA (cells) the FCT
+// limiter, TB (edges) the fluxes, TC (cells) the gathers and the q update.
+
+// TA (cells, FCT only): recomputes hProv, the bounds with the cells that hold
+// them, the upwind value and the limiter quotients of the stage
+// (apps/ocean/tasks/solve.cc:60-97, 194-267), and takes the cotangents of
+// R+ / R- that the limited fluxes of the cell's edges send back through the
+// factor each used (solve.cc:270-282) down to the bounds, upwind tendency,
+// flxIn / flxOut and hProv.
+__global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nC * L) return;
+  const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+  const int n = m.nEoC[c], T = a.T;
+  const double inva = m.invAreaCell[c], hin = a.h[i];
+  double th = 0.0;  // area-weighted thickness tendency of the stage input
+  for (int j = 0; j < n; ++j) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    const int e = m.eoc[s];
+    const int2 ce = m.coe[e];
+    const double F = a.u[(int64_t)e * L + k] * (0.5 * (a.h[(int64_t)ce.x * L + k] + a.h[(int64_t)ce.y * L + k]));
+    th = fma(m.eocSign[s] * m.dvEdge[e], F, th);
+  }
+  const double dtia = a.dt * inva;
+  const double hpi = 1.0 / fma(dtia, th, hin);
+  const double dthi = dtia * hpi;
+  const double eps = 1.e-10;
+  double lhpi = 0.0, lh = 0.0;
+  for (int t = 0; t < T; ++t) {
+    const int64_t it = i * T + t;
+    const double trc = a.tr[it], gc = a.lk_q[it] * inva;
+    const double2 own = a.R2[it];
+    double mx = trc, mn = trc, tl = 0.0, fi = 0.0, fo = 0.0, lrp = 0.0, lrm = 0.0;
+    int cmx = c, cmn = c;
+    for (int j = 0; j < n; ++j) {
+      const int64_t s = (int64_t)j * m.nC + c;
+      const int e = m.eoc[s];
+      const int64_t ie = ((int64_t)e * L + k) * T + t;
+      const double sg = m.eocSign[s], aa = a.A[ie];
+      tl = fma(sg, a.LO[ie], tl);
+      fi += dpos(sg * aa);
+      fo += dneg(sg * aa);
+      const int oc = m.coc[s];  // bounds in cellsOnCell order, strict comparisons (first wins ties)
+      const double x = a.tr[((int64_t)oc * L + k) * T + t];
+      if (x > mx) mx = x, cmx = oc;
+      if (x < mn) mn = x, cmn = oc;
+      // which of this cell's factors the limited flux of e used: A > 0 takes
+      // min(R-(c1), R+(c2)), A < 0 min(R+(c1), R-(c2)), the first on ties
+      const int nb = m.nbr[s];
+      const bool first = nb & 1;
+      const int64_t jo = ((int64_t)(nb >> 1) * L + k) * T + t;
+      const double2 ot = a.R2[jo];
+      const double go = a.lk_q[jo] * m.invAreaCell[nb >> 1];
+      const double ga = (first ? go - gc : gc - go) * aa;  // (g(c2) - g(c1)) A
+      if (dgt0(aa)) {
+        if (first) {
+          if (!(ot.x < own.y)) lrm += ga;
+        } else if (own.x < ot.y) {
+          lrp += ga;
+        }
+      } else if (dlt0(aa)) {
+        if (first) {
+          if (!(ot.y < own.x)) lrp += ga;
+        } else if (own.y < ot.x) {
+          lrm += ga;
+        }
+      }
+    }
+    const double num = fma(dtia, tl, trc * hin);
+    const double up = num * hpi;
+    const double np = mx - up, dp = fma(dthi, fi, eps);
+    const double nm = up - mn, dm = fma(-dthi, fo, eps);
+    double lup = 0.0, lmxv = 0.0, lmnv = 0.0, ldp = 0.0, ldm = 0.0;
+    // R = min(1, max(0, n / d)) passes a derivative only strictly inside (0, 1),
+    // read off the factor the forward computed
+    if (dgt0(own.x) && own.x < 1.0) {  // R+ = np / dp
+      const double r = 1.0 / dp, q = lrp * r;
+      lmxv = q, lup = -q, ldp = -q * np * r;
+    }
+    if (dgt0(own.y) && own.y < 1.0) {  // R- = nm / dm
+      const double r = 1.0 / dm, q = lrm * r;
+      lmnv = -q, lup += q, ldm = -q * nm * r;
+    }
+    a.lfi[it] = ldp * dthi;
+    a.lfo[it] = -ldm * dthi;
+    a.ltrs[it] = lup * hin * hpi;
+    a.ltl[it] = lup * dthi;
+    a.lmx[it] = lmxv, a.amx[it] = cmx;
+    a.lmn[it] = lmnv, a.amn[it] = cmn;
+    lh = fma(lup * trc, hpi, lh);
+    lhpi = fma(lup, num, lhpi);
+    lhpi = fma(fma(ldp, fi, -ldm * fo), dtia, lhpi);
+  }
+  // hProv = h + dt tend_h: its cotangent goes to h and to the thickness tendency
+  const double lhp = -lhpi * hpi * hpi;
+  a.muh_t[i] = lh + lhp;
+  a.lk_h[i] = fma(a.dt, lhp, a.lk_h[i]);
+}
+
+// TB (edges): the cotangents of the stage's edge fluxes.  FCT: the limited
+// antidiffusive flux A' and the cell sums (tLO, flxIn, flxOut) give A and LO;
+// LO = dv F tr_upwind and HO = F sum_a w_a tr_a (or the centred flux where the
+// high-order mask is 0) give F and the tracers (solve.cc:99-167, 216-229).
+// Without FCT: the centred flux of apps/sw/tasks/solve.cc:237-270.  del2
+// mixing (ocean solve.cc:328-366) adds to h_e and the tracers.  Per edge and
+// tracer, the parts for cells(e) go to p12 and lambda_HO F to lhof (TC
+// gathers them); per edge, the thickness-flux and edge-thickness cotangents
+// summed over tracers go to lFt / lhet (B1 adds them).
+__global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nE * L) return;
+  const int e = (int)(i / L), k = (int)(i - (int64_t)e * L), T = a.T;
+  const int2 c = m.coe[e];
+  const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
+  const double he = 0.5 * (a.h[i1] + a.h[i2]), F = a.u[i] * he, dv = m.dvEdge[e];
+  a.Ft[i] = F;
+  const double ia1 = m.invAreaCell[c.x], ia2 = m.invAreaCell[c.y];
+  const bool pos = dgt0(F), neg = dlt0(F);
+  const int mask = a.fct ? m.hoMask[(int64_t)e * m.fctLev + k] : 0;
+  const double kd = a.hmix ? a.kd[e] : 0.0;
+  double lF = 0.0, lhe = 0.0;
+  for (int t = 0; t < T; ++t) {
+    const int64_t i1t = i1 * T + t, i2t = i2 * T + t, it = i * T + t;
+    const double tr1 = a.tr[i1t], tr2 = a.tr[i2t];
+    const double G = a.lk_q[i2t] * ia2 - a.lk_q[i1t] * ia1;
+    double p1 = 0.0, p2 = 0.0;
+    if (a.fct) {
+      const double aa = a.A[it];
+      double lA = 0.0;
+      if (dgt0(aa)) {
+        const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
+        lA = fma(G, r2.x < r1.y ? r2.x : r1.y, a.lfi[i2t] - a.lfo[i1t]);
+      } else if (dlt0(aa)) {
+        const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
+        lA = fma(G, r2.y < r1.x ? r2.y : r1.x, a.lfo[i2t] - a.lfi[i1t]);
+      }
+      const double lLO = G + (a.ltl[i2t] - a.ltl[i1t]) - lA;
+      if (pos) {
+        lF = fma(lLO * dv, tr1, lF);
+        p1 = lLO * dv * F;
+      } else if (neg) {
+        lF = fma(lLO * dv, tr2, lF);
+        p2 = lLO * dv * F;
+      }
+      if (mask) {
+        double S = 0.0;
+        for (int sl = 0; sl < m.nAdv[e]; ++sl) {
+          const int64_t sa = (int64_t)sl * m.nE + e;
+          const double w = neg ? m.advCm[sa] : (pos ? m.advCp[sa] : m.advCoef[sa]);
+          S = fma(w, a.tr[((int64_t)m.advCells[sa] * L + k) * T + t], S);
+        }
+        lF = fma(lA, S, lF);
+        a.lhof[it] = lA * F;
+      } else {
+        const double hd = 0.5 * dv;
+        lF = fma(lA * hd, tr1 + tr2, lF);
+        const double q = lA * hd * F;
+        p1 += q, p2 += q;
+        a.lhof[it] = 0.0;
+      }
+    } else {
+      const double hd = 0.5 * dv;
+      lF = fma(G * hd, tr1 + tr2, lF);
+      p1 = p2 = G * hd * F;
+    }
+    if (a.hmix) {  // tend -= inva sum sign DF, DF = h_e (tr2 - tr1) kd
+      lhe = fma(-G * kd, tr2 - tr1, lhe);
+      const double q = G * he * kd;
+      p1 += q, p2 -= q;
+    }
+    a.p12[it] = make_double2(p1, p2);
+  }
+  a.lFt[i] = lF;
+  a.lhet[i] = lhe;
+}
+
+// TC (cells): the tracer cotangent of the stage input, gathered from the
+// upwind value, the edges of the cell, the advection stencils that read it
+// (DMesh::advR) and the bounds it holds for itself and its neighbours; then
+// q = h tr is converted and the RK bookkeeping of q runs.
+__global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nC * L) return;
+  const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+  const int n = m.nEoC[c], T = a.T;
+  const double hinv = 1.0 / a.h[i];
+  double mh = a.fct ? a.muh_t[i] : 0.0;
+  for (int t = 0; t < T; ++t) {
+    const int64_t it = i * T + t;
+    double lt = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int64_t s = (int64_t)j * m.nC + c;
+      const double2 p = a.p12[((int64_t)m.eoc[s] * L + k) * T + t];
+      lt += (m.nbr[s] & 1) ? p.x : p.y;
+    }
+    if (a.fct) {
+      lt += a.ltrs[it];
+      if (a.amx[it] == c) lt += a.lmx[it];
+      if (a.amn[it] == c) lt += a.lmn[it];
+      for (int j = 0; j < n; ++j) {  // each distinct neighbour once
+        const int oc = m.coc[(int64_t)j * m.nC + c];
+        bool dup = oc == c;
+        for (int p = 0; p < j && !dup; ++p) dup = m.coc[(int64_t)p * m.nC + c] == oc;
+        if (dup) continue;
+        const int64_t ot = ((int64_t)oc * L + k) * T + t;
+        if (a.amx[ot] == c) lt += a.lmx[ot];
+        if (a.amn[ot] == c) lt += a.lmn[ot];
+      }
+      for (int j = 0; j < m.maxAdvR; ++j) {
+        const int v = m.advR[(int64_t)j * m.nC + c];
+        if (v < 0) break;
+        const int e = v >> 4;
+        const int64_t sa = (int64_t)(v & 15) * m.nE + e, ie = (int64_t)e * L + k;
+        const double F = a.Ft[ie];
+        const double w = dlt0(F) ? m.advCm[sa] : (dgt0(F) ? m.advCp[sa] : m.advCoef[sa]);
+        lt = fma(w, a.lhof[ie * T + t], lt);
+      }
+    }
+    const double mq = lt * hinv;  // tr = q / h
+    mh = fma(-mq, a.tr[it], mh);
+    combine(a.rk, a.dt, it, mq, a.lam_q, a.acc_q, a.lk_q);
+  }
+  a.muh_t[i] = mh;
+}
+
+// Window ends: lambda_q = lambda_tr / h, lambda_h -= sum_t lambda_tr tr / h
+// (out = 0), and lambda_tr = lambda_q h, lambda_h += sum_t lambda_q tr (out = 1).
+__global__ void k_adj_q_convert(int64_t nCL, int T, const double *h, const double *tr, double *lam_q,
+                                double *lam_h, int out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nCL) return;
+  const double hi = h[i];
+  double lh = lam_h[i];
+  for (int t = 0; t < T; ++t) {
+    const int64_t it = i * T + t;
+    if (out) {
+      lh = fma(lam_q[it], tr[it], lh);
+      lam_q[it] *= hi;
+    } else {
+      const double q = lam_q[it] / hi;
+      lh = fma(-q, tr[it], lh);
+      lam_q[it] = q;
+    }
+  }
+  lam_h[i] = lh;
 }
 
 __global__ void k_adj_init(int64_t n, const double *lam, double *lk, double c) {
@@ -265,6 +564,17 @@ void ensure_buffers(SwState &s, int N, int k) {
       {(double **)&A->FP, 2 * eu}, {&A->pve, eu}, {&A->lam_u, eu}, {&A->lam_h, ch}, {&A->acc_u, eu},
       {&A->acc_h, ch}, {&A->lk_u, eu}, {&A->lk_h, ch}, {&A->mu_u, eu}, {&A->mu_h, ch}, {&A->lhe, eu},
       {&A->lpve, eu}, {&A->lke, ch}, {&A->ldiv, ch}, {&A->lcirc, vv}, {&A->lhs, vv}};
+  if (s.T > 0) {
+    const int64_t cT = ch * s.T, eT = eu * s.T;
+    const std::vector<std::pair<double **, int64_t>> tb = {
+        {&A->ck_tr, nck * cT}, {&A->tp_tr, (4LL * k + 1) * cT}, {&A->tp_A, 4LL * k * eT},
+        {&A->tp_LO, 4LL * k * eT}, {(double **)&A->tp_R2, 8LL * k * cT}, {&A->trhacc, cT},
+        {&A->lam_q, cT}, {&A->acc_q, cT}, {&A->lk_q, cT}, {&A->ltl, cT}, {&A->lfi, cT}, {&A->lfo, cT},
+        {&A->lmx, cT}, {&A->lmn, cT}, {&A->ltrs, cT}, {(double **)&A->amx, (cT + 1) / 2},
+        {(double **)&A->amn, (cT + 1) / 2}, {&A->muh_t, ch}, {&A->lFt, eu}, {&A->lhet, eu}, {&A->Ft, eu},
+        {&A->lhof, eT}, {(double **)&A->p12, 2 * eT}};
+    bufs.insert(bufs.end(), tb.begin(), tb.end());
+  }
   size_t total = 0;
   for (auto &b : bufs) total += ((size_t)std::max<int64_t>(b.second, 1) * 8 + 255) & ~size_t(255);
   if (cudaMalloc(&A->arena, total) != cudaSuccess) {
@@ -305,6 +615,21 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
   // plain stream order: programmatic dependent launch made this 25% slower (measured)
   const bool pdl = false;
   if (first) launch_pdl(k_adj_prep, nE, TPB, pdl, st, m, a, L);
+  if (A.tr) {
+    const int64_t cT = nC * s.T, eT = nE * s.T;
+    TrArgs t{};
+    t.u = a.u, t.h = a.h, t.tr = A.tp_tr + (size_t)j * cT;
+    t.A = A.tp_A + (size_t)j * eT, t.LO = A.tp_LO + (size_t)j * eT, t.R2 = A.tp_R2 + (size_t)j * cT;
+    t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
+    t.ltl = A.ltl, t.lfi = A.lfi, t.lfo = A.lfo, t.lmx = A.lmx, t.lmn = A.lmn, t.ltrs = A.ltrs;
+    t.amx = A.amx, t.amn = A.amn, t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.Ft = A.Ft;
+    t.lhof = A.lhof, t.p12 = A.p12;
+    t.T = s.T, t.rk = rk, t.fct = s.p.fct ? 1 : 0, t.hmix = s.p.hmix ? 1 : 0, t.dt = A.dt;
+    if (t.fct) launch_pdl(k_adj_tr_a, nC, TPB, pdl, st, m, t, L);
+    launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
+    launch_pdl(k_adj_tr_c, nC, TPB, pdl, st, m, t, L);
+    a.lFt = A.lFt, a.lhet = A.lhet, a.muh_t = A.muh_t;
+  }
   if (m.maxEoE == 10)
     launch_pdl(k_adj_b1<10>, nE, TPB, pdl, st, m, a, L);
   else
@@ -324,6 +649,8 @@ void forward(SwState &s, double dt, int N, int k) {
   A.N = N, A.k = k, A.dt = dt, A.nck = (N + k - 1) / k;
   MPASO_CUDA(cudaMemcpyAsync(A.ck_u, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
   MPASO_CUDA(cudaMemcpyAsync(A.ck_h, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+  const size_t ct = ch * s.T;
+  if (s.T) MPASO_CUDA(cudaMemcpyAsync(A.ck_tr, s.TR0, ct, cudaMemcpyDeviceToDevice, s.stream));
   for (int done = 0, c = 1; done < N; ++c) {
     const int n = std::min(k, N - done);
     sw_steps_graph(s, dt, n);
@@ -331,6 +658,9 @@ void forward(SwState &s, double dt, int N, int k) {
     if (done < N) {
       MPASO_CUDA(cudaMemcpyAsync(A.ck_u + (size_t)c * m.nE * s.L, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
       MPASO_CUDA(cudaMemcpyAsync(A.ck_h + (size_t)c * m.nC * s.L, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+      if (s.T)
+        MPASO_CUDA(cudaMemcpyAsync(A.ck_tr + (size_t)c * m.nC * s.L * s.T, s.TR0, ct, cudaMemcpyDeviceToDevice,
+                                   s.stream));
     }
   }
   A.have_forward = true;
@@ -340,14 +670,15 @@ void reverse_body(SwState &s) {
   AdjBuffers &A = *s.adj;
   const DMesh &m = s.mesh->ctx.d;
   const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
+  const int64_t cT = ch * s.T, eT = eu * s.T;
   const cudaStream_t st = s.stream;
-  k_adj_init<<<blocks_for(eu, TPB), TPB, 0, st>>>(eu, A.lam_u, A.lk_u, A.dt / 6);
-  k_adj_init<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, A.lam_h, A.lk_h, A.dt / 6);
   for (int seg = A.nck - 1; seg >= 0; --seg) {
     const int s0 = seg * A.k, n = std::min(A.k, A.N - s0);
     // taping recompute of the segment: slot 4t + rk holds the input of stage rk of step s0 + t
     MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
     MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
+    if (A.tr)
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, st));
     const int64_t vv = (int64_t)m.nV * s.L;
     sw_diag_ptrs(s, A.tp_u, A.tp_h, A.tp_pv, A.tp_hs, st);
     for (int t = 0; t < n; ++t) {
@@ -356,10 +687,37 @@ void reverse_body(SwState &s) {
         double *iu = yu + (size_t)rk * eu, *ih = yh + (size_t)rk * ch;
         double *ou = yu + (size_t)(rk + 1) * eu, *oh = yh + (size_t)(rk + 1) * ch;
         const size_t next = (size_t)(4 * t + rk + 1) * vv;  // tape slot of the stage's output
-        sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc,
-                      A.hacc, rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next,
-                      A.tp_hs + next, st);
+        if (!A.tr) {
+          sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc,
+                        A.hacc, rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next,
+                        A.tp_hs + next, st);
+          continue;
+        }
+        // with tracers: the state's own stage kernels, every pointer on the tape
+        const int j = 4 * t + rk;
+        double *ytr = A.tp_tr + (size_t)4 * t * cT;
+        Stage S = sw_make_stage(s, rk, A.dt);
+        S.u_in = iu, S.h_in = ih, S.tr_in = ytr + (size_t)rk * cT;
+        S.u_prev = yu, S.h_prev = yh, S.tr_prev = ytr;
+        S.u_out = rk < 3 ? ou : nullptr, S.h_out = rk < 3 ? oh : nullptr;
+        S.tr_out = rk < 3 ? ytr + (size_t)(rk + 1) * cT : nullptr;
+        S.u_acc = A.uacc, S.h_acc = A.hacc, S.trh_acc = A.trhacc;
+        S.u_new = rk == 3 ? ou : nullptr, S.h_new = rk == 3 ? oh : nullptr;
+        S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
+        S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
+        S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next;
+        sw_launch_stage(s, S, st);
       }
+    }
+    if (seg == A.nck - 1) {
+      // cotangents of the final state (tape slot 4n): tracers to q = h tr, then
+      // the first reversed stage's lk = dt/6 lam
+      if (A.tr)
+        k_adj_q_convert<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, s.T, A.tp_h + (size_t)4 * n * ch,
+                                                              A.tp_tr + (size_t)4 * n * cT, A.lam_q, A.lam_h, 0);
+      k_adj_init<<<blocks_for(eu, TPB), TPB, 0, st>>>(eu, A.lam_u, A.lk_u, A.dt / 6);
+      k_adj_init<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, A.lam_h, A.lk_h, A.dt / 6);
+      if (A.tr) k_adj_init<<<blocks_for(cT, TPB), TPB, 0, st>>>(cT, A.lam_q, A.lk_q, A.dt / 6);
     }
     for (int t = n - 1; t >= 0; --t)
       for (int rk = 3; rk >= 0; --rk) {
@@ -367,6 +725,9 @@ void reverse_body(SwState &s) {
         stage_vjp(s, A, rk, j, t == n - 1 && rk == 3, j > 0, st);
       }
   }
+  // q = h tr at the window's start (tape slot 0 holds checkpoint 0)
+  if (A.tr)
+    k_adj_q_convert<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, s.T, A.tp_h, A.tp_tr, A.lam_q, A.lam_h, 1);
   MPASO_CUDA(cudaGetLastError());
 }
 
@@ -374,7 +735,7 @@ void reverse_body(SwState &s) {
 // once as a graph for the current (N, k, dt) and buffers, then replayed.
 void reverse(SwState &s) {
   AdjBuffers &A = *s.adj;
-  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt)) drop_adjoint_graph(s);
+  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt || A.rev_tr != A.tr)) drop_adjoint_graph(s);
   if (!A.rev) {
     cudaGraph_t g;
     MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
@@ -389,35 +750,36 @@ void reverse(SwState &s) {
     const cudaError_t e = cudaGraphInstantiate(&A.rev, g, 0);
     cudaGraphDestroy(g);
     MPASO_CUDA(e);
-    A.rev_N = A.N, A.rev_k = A.k, A.rev_dt = A.dt;
+    A.rev_N = A.N, A.rev_k = A.k, A.rev_dt = A.dt, A.rev_tr = A.tr;
   }
   MPASO_CUDA(cudaGraphLaunch(A.rev, s.stream));
   s.diag_valid = false;
 }
 
-void to_internal(SwState &s, const double *src, double *dst, int entity) {
+// Reference-ordered rows of `row` doubles (host or device) <-> internal order.
+void to_internal(SwState &s, const double *src, double *dst, int entity, int64_t row) {
   MeshCtx &ctx = s.mesh->ctx;
   const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : ctx.d.nE;
   const double *p = src;
   double *stage = nullptr;
   if (!is_device_pointer(src)) {
-    MPASO_CUDA(cudaMallocAsync((void **)&stage, (size_t)n * s.L * 8, s.stream));
-    MPASO_CUDA(cudaMemcpyAsync(stage, src, (size_t)n * s.L * 8, cudaMemcpyHostToDevice, s.stream));
+    MPASO_CUDA(cudaMallocAsync((void **)&stage, (size_t)n * row * 8, s.stream));
+    MPASO_CUDA(cudaMemcpyAsync(stage, src, (size_t)n * row * 8, cudaMemcpyHostToDevice, s.stream));
     p = stage;
   }
-  k_gather_rows_pub(p, dst, ctx.d_perm[entity], n, s.L, s.stream);
+  k_gather_rows_pub(p, dst, ctx.d_perm[entity], n, row, s.stream);
   if (stage) MPASO_CUDA(cudaFreeAsync(stage, s.stream));
 }
 
-void from_internal(SwState &s, const double *src, double *dst, int entity) {
+void from_internal(SwState &s, const double *src, double *dst, int entity, int64_t row) {
   MeshCtx &ctx = s.mesh->ctx;
   const int64_t n = entity == MPASO_CELLS ? ctx.d.nC : ctx.d.nE;
   const bool dev = is_device_pointer(dst);
   double *out = dst;
-  if (!dev) MPASO_CUDA(cudaMallocAsync((void **)&out, (size_t)n * s.L * 8, s.stream));
-  k_scatter_rows_pub(src, out, ctx.d_perm[entity], n, s.L, s.stream);
+  if (!dev) MPASO_CUDA(cudaMallocAsync((void **)&out, (size_t)n * row * 8, s.stream));
+  k_scatter_rows_pub(src, out, ctx.d_perm[entity], n, row, s.stream);
   if (!dev) {
-    MPASO_CUDA(cudaMemcpyAsync(dst, out, (size_t)n * s.L * 8, cudaMemcpyDeviceToHost, s.stream));
+    MPASO_CUDA(cudaMemcpyAsync(dst, out, (size_t)n * row * 8, cudaMemcpyDeviceToHost, s.stream));
     MPASO_CUDA(cudaFreeAsync(out, s.stream));
   }
 }
@@ -443,11 +805,35 @@ int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0
     SwState &S = s->s;
     require(S.adj && S.adj->have_forward, MPASO_ERR_ARG, "mpaso_rk4_vjp needs a preceding mpaso_rk4_forward");
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
-    to_internal(S, gu, S.adj->lam_u, MPASO_EDGES);
-    to_internal(S, gh, S.adj->lam_h, MPASO_CELLS);
+    to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);
+    to_internal(S, gh, S.adj->lam_h, MPASO_CELLS, S.L);
+    S.adj->tr = 0;
     reverse(S);
-    from_internal(S, S.adj->lam_u, gu0, MPASO_EDGES);
-    from_internal(S, S.adj->lam_h, gh0, MPASO_CELLS);
+    from_internal(S, S.adj->lam_u, gu0, MPASO_EDGES, S.L);
+    from_internal(S, S.adj->lam_h, gh0, MPASO_CELLS, S.L);
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+  });
+}
+
+int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, const double *gtr, double *gh0,
+                          double *gu0, double *gtr0) {
+  return guarded("mpaso_rk4_vjp_tracers", [&] {
+    require(s && gh && gu && gtr && gh0 && gu0 && gtr0, MPASO_ERR_ARG, "null argument");
+    SwState &S = s->s;
+    require(S.T > 0, MPASO_ERR_ARG, "mpaso_rk4_vjp_tracers needs a state with tracers");
+    require(S.adj && S.adj->have_forward, MPASO_ERR_ARG,
+            "mpaso_rk4_vjp_tracers needs a preceding mpaso_rk4_forward");
+    require(!S.p.fct || S.mesh->ctx.has_fct, MPASO_ERR_ARG, "FCT statics missing from the mesh");
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    const int64_t LT = (int64_t)S.L * S.T;
+    to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);
+    to_internal(S, gh, S.adj->lam_h, MPASO_CELLS, S.L);
+    to_internal(S, gtr, S.adj->lam_q, MPASO_CELLS, LT);
+    S.adj->tr = 1;
+    reverse(S);
+    from_internal(S, S.adj->lam_u, gu0, MPASO_EDGES, S.L);
+    from_internal(S, S.adj->lam_h, gh0, MPASO_CELLS, S.L);
+    from_internal(S, S.adj->lam_q, gtr0, MPASO_CELLS, LT);
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
   });
 }

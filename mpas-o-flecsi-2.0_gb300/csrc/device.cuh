@@ -71,6 +71,10 @@ struct DMesh {
   const double *woeT;         // [maxEoE][nE] weight of e in the stencil of eoe[j][e] (0 in pads)
   const int *vocR;            // [maxEoC][nC] vertices of c (pads repeat slot 0)
   const double *kiteR;        // [maxEoC][nC] kite of c at vocR[j][c] (0 in pads)
+  // [maxAdvR][nC] (edge << 4) | slot of every advection stencil entry that
+  // reads the cell (advCells[slot][edge] == c), ascending edge, -1 pads last
+  const int *advR;
+  int maxAdvR;
 };
 
 // Host-side mesh context.

@@ -343,6 +343,18 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   for (int64_t c = 0; c < nC; ++c)
     for (int j = fillc[c]; j < maxEoC; ++j) vocR[(size_t)j * nC + c] = vocR[c];
   A.add(woeT, &m.woeT), A.add(vocR, &m.vocR), A.add(kiteR, &m.kiteR);
+  // cell -> (edge, slot) entries of the advection stencils that read the cell,
+  // (edge << 4) | slot, ascending edge; -1 pads at the end of each column
+  std::vector<std::vector<int>> rev(ctx.has_fct ? nC : 0);
+  for (int64_t k = 0; ctx.has_fct && k < nE; ++k)
+    for (int j = 0; j < nAdv[k]; ++j) rev[advCells[(size_t)j * nE + k]].push_back((int)(k << 4) | j);
+  int maxAdvR = 1;
+  for (auto &r : rev) maxAdvR = std::max(maxAdvR, (int)r.size());
+  std::vector<int> advR((size_t)maxAdvR * nC, -1);
+  for (size_t c = 0; c < rev.size(); ++c)
+    for (size_t j = 0; j < rev[c].size(); ++j) advR[j * nC + c] = rev[c][j];
+  m.maxAdvR = maxAdvR;
+  A.add(advR, &m.advR);
 
   A.upload(ctx);
   ctx.perm[0] = pc, ctx.perm[1] = pe, ctx.perm[2] = pv;

@@ -573,6 +573,11 @@ void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const doub
   launch_stage_T<0>(s, S, st);
 }
 
+// A stage with the state's weights and buffers, for callers that redirect
+// some of its pointers (the adjoint's taping recompute with tracers).
+Stage sw_make_stage(SwState &s, int rk, double dt) { return make_stage(s, rk, dt); }
+void sw_launch_stage(SwState &s, const Stage &S, cudaStream_t st) { launch_stage(s, S, st); }
+
 // Diagnostics (pv, vorticity, ke, divergence) of an explicit (u, h); pv and the
 // kite-summed thickness also go to tape_pv / tape_hs when given.
 void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv, double *tape_hs,

@@ -178,6 +178,8 @@ void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv,
 void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
 // nsteps graph-replayed steps on the state's stream (the step graph is cached)
 void sw_steps_graph(SwState &s, double dt, int nsteps);
+Stage sw_make_stage(SwState &s, int rk, double dt);
+void sw_launch_stage(SwState &s, const Stage &S, cudaStream_t st);
 void drop_adjoint_graph(SwState &s);
 
 // ---------------------------------------------------------------------------

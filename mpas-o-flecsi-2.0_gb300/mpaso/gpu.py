@@ -328,6 +328,17 @@ class State:
         check(lib().mpaso_rk4_vjp(self._h, _ptr(gh), _ptr(gu), _ptr(gh0), _ptr(gu0)))
         return gh0, gu0
 
+    def vjp_tracers(self, gh, gu, gtr, out=None):
+        """Cotangents of the initial (h, u, tracers) from cotangents of the final (h, u, tracers)
+        of the last forward; the FCT limiter is differentiated on the branch the forward took."""
+        gh0, gu0, gtr0 = out if out is not None else (
+            np.empty(self._shape(FIELD_H)), np.empty(self._shape(FIELD_U)), np.empty(self._shape(FIELD_TRACERS)))
+        gh, gu, gtr = (np.ascontiguousarray(x, np.float64) if isinstance(x, np.ndarray) else x
+                       for x in (gh, gu, gtr))
+        check(lib().mpaso_rk4_vjp_tracers(self._h, _ptr(gh), _ptr(gu), _ptr(gtr), _ptr(gh0), _ptr(gu0),
+                                          _ptr(gtr0)))
+        return gh0, gu0, gtr0
+
     def adjoint_device_bytes(self):
         b = ctypes.c_int64()
         check(lib().mpaso_adjoint_device_bytes(self._h, ctypes.byref(b)))

@@ -24,8 +24,21 @@ differs)."""
 import numpy as np
 
 
+def _smax(a, b):
+    """(a < b) ? b : a on the real parts (the reference's max), carrying the chosen value."""
+    return np.where(np.real(a) < np.real(b), b, a)
+
+
+def _smin(a, b):
+    """(b < a) ? b : a on the real parts (the reference's min)."""
+    return np.where(np.real(b) < np.real(a), b, a)
+
+
 class SwComplex:
-    def __init__(self, mesh, L, gravity=9.80616, nu=0.0, bottomDepth=None):
+    def __init__(self, mesh, L, gravity=9.80616, nu=0.0, bottomDepth=None, fct=None, T=0,
+                 hmix=False, kappa=0.0, centred=False):
+        """fct: the FCT statics (edge signs, advection stencils, del2 scaling), or None;
+        centred: the sw app's centred tracer flux even when statics are given."""
         f = mesh.fields
         crs = mesh.crs()
         self.nC, self.nE, self.nV, self.L = mesh.nCells, mesh.nEdges, mesh.nVertices, L
@@ -57,6 +70,25 @@ class SwComplex:
         self.kite = f["kiteAreasOnVertex"]
         self.fv = f["fVertex"][:, None]
         self.bd = (np.zeros(self.nC) if bottomDepth is None else np.asarray(bottomDepth, float))[:, None]
+        # tracers: FCT advection (apps/ocean/tasks/solve.cc:99-326) and del2 mixing (:328-366),
+        # thickness-weighted RK of apps/sw/tasks/solve.cc:162, 300-302, 337, 354
+        self.T, self.hmix, self.kappa, self.fct = T, hmix, kappa, fct is not None and not centred
+        self.c2c_c = np.repeat(np.arange(self.nC), np.diff(crs["c2c"][0]))
+        self.c2c_n = crs["c2c"][1]
+        slot_e = np.arange(ci.size) - np.repeat(co[:-1], np.diff(co))
+        if fct is not None:
+            self.esgn = fct["edgeSignOnCell"][self.c2e_c, slot_e][:, None, None]
+            na = fct["nAdvCellsForEdge"]
+            ea = np.repeat(np.arange(self.nE), na)
+            sa = np.arange(na.sum()) - np.repeat(np.cumsum(na) - na, na)
+            self.adv_e, self.adv_c = ea, fct["advCellsForEdge"][ea, sa]
+            self.adv_c1 = fct["advCoef"][ea, sa][:, None, None]
+            self.adv_c3 = (fct["advCoef_3rd"][ea, sa] * 0.25)[:, None, None]
+            self.mask = fct["highOrderAdvMask"][:, :L].astype(float)[:, :, None]
+            self.msd = fct["meshScalingDel2"][:, None, None]
+        else:
+            self.esgn = np.where(self.c1[ci] == self.c2e_c, -1.0, 1.0)[:, None, None]
+            self.msd = np.ones((self.nE, 1, 1))
 
     def _scatter(self, n, idx, vals):
         out = np.zeros((n, self.L), vals.dtype)
@@ -90,22 +122,103 @@ class SwComplex:
             tend_u = tend_u + self.nu * ((div[c2] - div[c1]) / self.dc - (vort[self.v2] - vort[self.v1]) / self.dv)
         return tend_h, tend_u
 
-    def step(self, h, u, dt, nsteps=1):
-        """nsteps RK4 steps (apps/sw/run.cc:13-70); h (nC, L), u (nE, L)."""
+    def tracer_tendency(self, h, u, tr, dt):
+        """Tracer mass tendency [nC][L][T] of a stage state (FCT of apps/ocean/tasks/
+        solve.cc:99-326 on the sw thickness flux, plus del2 mixing of :328-366)."""
+        c1, c2 = self.c1, self.c2
+        he = 0.5 * (h[c1] + h[c2])
+        ntf = (u * he)[:, :, None]                                     # normal thickness flux
+        dv = self.dv[:, :, None]
+        ce, ee = self.c2e_c, self.c2e_e
+        sgn_area = self.esgn / self.area[ce][:, :, None]
+        if self.fct:
+            # provisional thickness and its inverse
+            hprov = h + self._scatter(self.nC, ce, (dt * self.dv[ee] * self.esgn[:, :, 0] / self.area[ce])
+                                      * (u * he)[ee])
+            hpi = (1.0 / hprov)[:, :, None]
+            lo = dv * (_smax(0.0, ntf) * tr[c1] + _smin(0.0, ntf) * tr[c2])
+            f = ntf[self.adv_e]
+            sg = np.where(np.real(f) < 0, -1.0, np.where(np.real(f) > 0, 1.0, 0.0))
+            wf = f * self.mask[self.adv_e] * (self.adv_c1 + self.adv_c3 * sg)
+            ho = np.zeros(lo.shape, np.result_type(lo, wf))
+            np.add.at(ho, self.adv_e, tr[self.adv_c] * wf)
+            ho = ho + (1.0 - self.mask) * (dv * 0.5) * ntf * (tr[c1] + tr[c2])
+            ho = ho - lo
+            # bounds over the cell and its neighbours, taken in the cell->cell list's order
+            trmax, trmin = tr.copy(), tr.copy()
+            nn = self.c2c_n
+            cnt = np.bincount(self.c2c_c, minlength=self.nC)
+            start = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+            for j in range(cnt.max()):
+                sel = cnt > j
+                cells = np.nonzero(sel)[0]
+                nb = nn[start[sel] + j]
+                trmax[cells] = _smax(trmax[cells], tr[nb])
+                trmin[cells] = _smin(trmin[cells], tr[nb])
+            tend_lo = self._scatter3(ce, sgn_area * lo[ee])
+            fin = self._scatter3(ce, _smax(0.0, sgn_area * ho[ee]))
+            fout = self._scatter3(ce, _smin(0.0, sgn_area * ho[ee]))
+            upw = (tr * h[:, :, None] + dt * tend_lo) * hpi
+            tmax_new = upw + dt * fin * hpi
+            tmin_new = upw + dt * fout * hpi
+            eps = 1.e-10
+            rp = _smin(1.0, _smax(0.0, (trmax - upw) / (tmax_new - upw + eps)))
+            rm = _smin(1.0, _smax(0.0, (upw - trmin) / (upw - tmin_new + eps)))
+            hol = _smax(0.0, ho) * _smin(rm[c1], rp[c2]) + _smin(0.0, ho) * _smin(rp[c1], rm[c2])
+            np.add.at(tend_lo, ce, sgn_area * hol[ee])
+            tend = tend_lo
+        else:  # centred flux (apps/sw/tasks/solve.cc:237-270)
+            flux = dv * ntf * (0.5 * (tr[c1] + tr[c2]))
+            tend = self._scatter3(c2, flux / self.area[c2][:, :, None]) - \
+                self._scatter3(c1, flux / self.area[c1][:, :, None])
+        if self.hmix:
+            rho = self.msd * self.kappa * dv / self.dc[:, :, None]
+            fl = he[:, :, None] * (tr[c2] - tr[c1]) * rho
+            tend = tend - self._scatter3(ce, sgn_area * fl[ee])
+        return tend
+
+    def _scatter3(self, idx, vals):
+        out = np.zeros((self.nC, self.L, self.T), vals.dtype)
+        np.add.at(out, idx, vals)
+        return out
+
+    def step(self, h, u, dt, nsteps=1, tr=None):
+        """nsteps RK4 steps (apps/sw/run.cc:13-70); h (nC, L), u (nE, L), tr (nC, L, T) or None."""
         h = np.asarray(h).reshape(self.nC, self.L)
         u = np.asarray(u).reshape(self.nE, self.L)
+        if tr is not None:
+            tr = np.asarray(tr).reshape(self.nC, self.L, self.T)
         w = (dt / 6, dt / 3, dt / 3, dt / 6)
         sub = (dt / 2, dt / 2, dt)
         for _ in range(nsteps):
-            hp, up = h, u
+            hp, up, tp = h, u, tr
             hn, un = h.copy(), u.copy()
+            qn = None if tr is None else tr * h[:, :, None]
             for rk in range(4):
                 th, tu = self.tendencies(hp, up)
+                tq = None if tr is None else self.tracer_tendency(hp, up, tp, dt)
                 if rk < 3:
                     hp, up = h + sub[rk] * th, u + sub[rk] * tu
+                    if tr is not None:
+                        tp = (h[:, :, None] * tr + sub[rk] * tq) / hp[:, :, None]
                 hn, un = hn + w[rk] * th, un + w[rk] * tu
+                if tr is not None:
+                    qn = qn + w[rk] * tq
             h, u = hn, un
-        return h, u
+            if tr is not None:
+                tr = qn / hn[:, :, None]
+        return (h, u) if tr is None else (h, u, tr)
+
+    def jvp_tracers(self, h, u, tr, vh, vu, vt, dt, nsteps, eps=1e-30):
+        """Directional derivative of (h_N, u_N, tr_N) along (vh, vu, vt) by the complex step;
+        every max / min / sign of the FCT limiter is decided on the real parts, so this is the
+        derivative on the branch the real step takes."""
+        hc = np.asarray(h, complex).reshape(self.nC, self.L) + 1j * eps * np.asarray(vh).reshape(self.nC, self.L)
+        uc = np.asarray(u, complex).reshape(self.nE, self.L) + 1j * eps * np.asarray(vu).reshape(self.nE, self.L)
+        tc = (np.asarray(tr, complex).reshape(self.nC, self.L, self.T)
+              + 1j * eps * np.asarray(vt).reshape(self.nC, self.L, self.T))
+        hN, uN, tN = self.step(hc, uc, dt, nsteps, tr=tc)
+        return hN.imag / eps, uN.imag / eps, tN.imag / eps
 
     def jvp(self, h, u, vh, vu, dt, nsteps, eps=1e-30):
         """Directional derivative of (h_N, u_N) along (vh, vu) by the complex step."""
