@@ -69,12 +69,15 @@ struct AdjBuffers {
   double *ck_tr = nullptr, *tp_tr = nullptr;  // [nck][nC L T], [4k + 1][nC L T]
   double *tp_A = nullptr, *tp_LO = nullptr;   // [4k][nE L T]
   double2 *tp_R2 = nullptr;                   // [4k][nC L T] {R+, R-}
+  double *tp_tLO = nullptr;                   // [4k][nC L T] area-weighted upwind sums
+  double *tp_hpi = nullptr;                   // [4k][nC L] 1/hProv
   double *trhacc = nullptr;
-  double *lam_q = nullptr, *acc_q = nullptr, *lk_q = nullptr;
-  double *ltl = nullptr, *lfi = nullptr, *lfo = nullptr, *lmx = nullptr, *lmn = nullptr, *ltrs = nullptr;
-  int *amx = nullptr, *amn = nullptr;
-  double *muh_t = nullptr, *lFt = nullptr, *lhet = nullptr, *Ft = nullptr, *lhof = nullptr;
-  double2 *p12 = nullptr;
+  double *lam_q = nullptr, *acc_q = nullptr, *lk_q = nullptr, *gq = nullptr;
+  double *ltl = nullptr, *ltrs = nullptr;
+  double2 *lfio = nullptr, *lmm = nullptr;
+  int2 *amm = nullptr;
+  double *muh_t = nullptr, *lFt = nullptr, *lhet = nullptr;
+  double2 *p12 = nullptr, *lho = nullptr;
   // the whole reverse sweep, captured once per (N, k, dt, tracers) and replayed
   cudaGraphExec_t rev = nullptr;
   int rev_N = 0, rev_k = 0, rev_tr = 0;
@@ -123,13 +126,15 @@ struct TrArgs {
   const double *u, *h, *tr;        // stage input (tape)
   const double *A, *LO;            // stage fluxes (tape)
   const double2 *R2;               // stage limiter factors (tape)
+  const double *hpi, *tLO;         // stage 1/hProv and area-weighted upwind sum (tape)
   const double *kd;                // del2 coefficient per edge
   double *lk_h;                    // thickness-tendency cotangent, + dt lambda_hProv in place
-  double *lk_q, *lam_q, *acc_q;
-  double *ltl, *lfi, *lfo, *lmx, *lmn, *ltrs;
-  int *amx, *amn;
-  double *muh_t, *lFt, *lhet, *Ft, *lhof;
-  double2 *p12;
+  double *lk_q, *gq, *lam_q, *acc_q;
+  double *ltl, *ltrs;              // per cell and tracer: upwind-sum and own-tracer cotangents
+  double2 *lfio, *lmm;             // {flxIn, flxOut} and {max, min} bound cotangents
+  int2 *amm;                       // cells holding the {max, min} bound
+  double *muh_t, *lFt, *lhet;
+  double2 *p12, *lho;              // per edge and tracer: parts for cells(e); lambda_HO F by sign of F
   int T, rk, fct, hmix;
   double dt;
 };
@@ -299,97 +304,124 @@ __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, in
 // ---------------------------------------------------------------------------
 // Tracer reverse, three launches per stage ahead of B1: TA (cells) the FCT
 // limiter, TB (edges) the fluxes, TC (cells) the gathers and the q update.
+// g = lk_q / areaCell is kept beside lk_q (the tendency's per-area cotangent).
 
-// TA (cells, FCT only): recomputes hProv, the bounds with the cells that hold
-// them, the upwind value and the limiter quotients of the stage
-// (apps/ocean/tasks/solve.cc:60-97, 194-267), and takes the cotangents of
-// R+ / R- that the limited fluxes of the cell's edges send back through the
-// factor each used (solve.cc:270-282) down to the bounds, upwind tendency,
-// flxIn / flxOut and hProv.
+// The NL lanes of a cell are adjacent and NL-aligned in a warp; kernels
+// retire whole groups, so a group's mask names live threads only.
+template <int NL> __device__ __forceinline__ unsigned group_mask() {
+  return ((1u << NL) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(NL - 1));
+}
+
+// Sum over the NL lanes of a cell.
+template <int NL> __device__ __forceinline__ double lane_sum(double v) {
+  const unsigned gm = group_mask<NL>();
+#pragma unroll
+  for (int o = NL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gm, v, o);
+  return v;
+}
+
+// TA (cells, FCT only): the bounds with the cells that hold them, the upwind
+// value and the limiter quotients of the stage (apps/ocean/tasks/solve.cc:
+// 194-267; 1/hProv and the upwind sum are taped by the recompute), and the
+// cotangents of R+ / R- that the limited fluxes of the cell's edges send back
+// through the factor each used (solve.cc:270-282), taken down to the bounds,
+// the upwind sum, flxIn / flxOut and hProv.  NL lanes per cell share its edge
+// slots; the bounds merge as (value, slot) with the lower slot (the cell
+// itself first) winning ties, which is the reference's sequential max / min.
+template <int NL, int NC>
 __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= (int64_t)m.nC * L) return;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = (int)(g & (NL - 1));
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (g / NL >= nCL) return;  // whole groups: all lanes of a live cell stay
+  const int64_t i = g / NL;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c], T = a.T;
-  const double inva = m.invAreaCell[c], hin = a.h[i];
-  double th = 0.0;  // area-weighted thickness tendency of the stage input
-  for (int j = 0; j < n; ++j) {
-    const int64_t s = (int64_t)j * m.nC + c;
-    const int e = m.eoc[s];
-    const int2 ce = m.coe[e];
-    const double F = a.u[(int64_t)e * L + k] * (0.5 * (a.h[(int64_t)ce.x * L + k] + a.h[(int64_t)ce.y * L + k]));
-    th = fma(m.eocSign[s] * m.dvEdge[e], F, th);
-  }
-  const double dtia = a.dt * inva;
-  const double hpi = 1.0 / fma(dtia, th, hin);
+  const double hin = a.h[i], hpi = a.hpi[i];
+  const double dtia = a.dt * m.invAreaCell[c];
   const double dthi = dtia * hpi;
   const double eps = 1.e-10;
   double lhpi = 0.0, lh = 0.0;
   for (int t = 0; t < T; ++t) {
     const int64_t it = i * T + t;
-    const double trc = a.tr[it], gc = a.lk_q[it] * inva;
+    const double trc = a.tr[it], gc = a.gq[it];
     const double2 own = a.R2[it];
-    double mx = trc, mn = trc, tl = 0.0, fi = 0.0, fo = 0.0, lrp = 0.0, lrm = 0.0;
-    int cmx = c, cmn = c;
-    for (int j = 0; j < n; ++j) {
+    double mx = trc, mn = trc, fi = 0.0, fo = 0.0, lrp = 0.0, lrm = 0.0;
+    int smx = -1, smn = -1;
+    auto slot = [&](int j, bool ok) {
+      // compares, selects and sign flips on the integer pipe (rk4.cuh helpers),
+      // one add per slot for flxIn / flxOut; pad slots (own cell, slot-0 edge)
+      // are masked and cannot win a bound
       const int64_t s = (int64_t)j * m.nC + c;
-      const int e = m.eoc[s];
-      const int64_t ie = ((int64_t)e * L + k) * T + t;
-      const double sg = m.eocSign[s], aa = a.A[ie];
-      tl = fma(sg, a.LO[ie], tl);
-      fi += dpos(sg * aa);
-      fo += dneg(sg * aa);
-      const int oc = m.coc[s];  // bounds in cellsOnCell order, strict comparisons (first wins ties)
-      const double x = a.tr[((int64_t)oc * L + k) * T + t];
-      if (x > mx) mx = x, cmx = oc;
-      if (x < mn) mn = x, cmn = oc;
+      const double aa = a.A[((int64_t)m.eoc[s] * L + k) * T + t];
+      const double sa = dmask(dflip(aa, sign_mask(m.eocSign[s])), ok);
+      const bool in = dgt0(sa);
+      const double f = (in ? fi : fo) + sa;
+      fi = in ? f : fi, fo = in ? fo : f;
+      const double x = a.tr[((int64_t)m.coc[s] * L + k) * T + t];
+      if (dkey(mx) < dkey(x)) mx = x, smx = j;
+      if (dkey(x) < dkey(mn)) mn = x, smn = j;
       // which of this cell's factors the limited flux of e used: A > 0 takes
       // min(R-(c1), R+(c2)), A < 0 min(R+(c1), R-(c2)), the first on ties
       const int nb = m.nbr[s];
       const bool first = nb & 1;
       const int64_t jo = ((int64_t)(nb >> 1) * L + k) * T + t;
       const double2 ot = a.R2[jo];
-      const double go = a.lk_q[jo] * m.invAreaCell[nb >> 1];
-      const double ga = (first ? go - gc : gc - go) * aa;  // (g(c2) - g(c1)) A
-      if (dgt0(aa)) {
-        if (first) {
-          if (!(ot.x < own.y)) lrm += ga;
-        } else if (own.x < ot.y) {
-          lrp += ga;
-        }
-      } else if (dlt0(aa)) {
-        if (first) {
-          if (!(ot.y < own.x)) lrp += ga;
-        } else if (own.y < ot.x) {
-          lrm += ga;
-        }
+      int sel = 0;  // 1: R+ of this cell, 2: R- of this cell
+      if (!ok)
+        ;
+      else if (dgt0(aa))
+        sel = first ? (dkey(ot.x) < dkey(own.y) ? 0 : 2) : (dkey(own.x) < dkey(ot.y) ? 1 : 0);
+      else if (dlt0(aa))
+        sel = first ? (dkey(ot.y) < dkey(own.x) ? 0 : 1) : (dkey(own.y) < dkey(ot.x) ? 2 : 0);
+      if (sel) {
+        const double go = a.gq[jo];
+        const double G = first ? go - gc : gc - go;  // g(c2) - g(c1)
+        if (sel == 1)
+          lrp = fma(G, aa, lrp);
+        else
+          lrm = fma(G, aa, lrm);
       }
+    };
+    if constexpr (NL == 1)
+      for_slots<NC>(n, slot);
+    else
+      for (int j = lane; j < n; j += NL) slot(j, true);
+    const unsigned gm = group_mask<NL>();
+#pragma unroll
+    for (int o = NL / 2; o > 0; o >>= 1) {
+      const double xm = __shfl_xor_sync(gm, mx, o), xn = __shfl_xor_sync(gm, mn, o);
+      const int sm = __shfl_xor_sync(gm, smx, o), sn = __shfl_xor_sync(gm, smn, o);
+      if (dkey(mx) < dkey(xm) || (dkey(xm) == dkey(mx) && sm < smx)) mx = xm, smx = sm;
+      if (dkey(xn) < dkey(mn) || (dkey(xn) == dkey(mn) && sn < smn)) mn = xn, smn = sn;
     }
-    const double num = fma(dtia, tl, trc * hin);
+    fi = lane_sum<NL>(fi), fo = lane_sum<NL>(fo), lrp = lane_sum<NL>(lrp), lrm = lane_sum<NL>(lrm);
+    if (lane) continue;
+    const double num = fma(dtia, a.tLO[it], trc * hin);
     const double up = num * hpi;
-    const double np = mx - up, dp = fma(dthi, fi, eps);
-    const double nm = up - mn, dm = fma(-dthi, fo, eps);
-    double lup = 0.0, lmxv = 0.0, lmnv = 0.0, ldp = 0.0, ldm = 0.0;
+    double lup = 0.0, ldp = 0.0, ldm = 0.0;
+    double2 lb = make_double2(0.0, 0.0);  // cotangents of the max / min bounds
     // R = min(1, max(0, n / d)) passes a derivative only strictly inside (0, 1),
     // read off the factor the forward computed
-    if (dgt0(own.x) && own.x < 1.0) {  // R+ = np / dp
-      const double r = 1.0 / dp, q = lrp * r;
-      lmxv = q, lup = -q, ldp = -q * np * r;
+    constexpr long long kOne = 0x3ff0000000000000LL;
+    if (dgt0(own.x) && dkey(own.x) < kOne) {  // R+ = (max - up) / (dthi flxIn + eps)
+      const double dp = fma(dthi, fi, eps), r = rcp_nr(dp), q = lrp * r;
+      lb.x = q, lup = -q, ldp = -q * (mx - up) * r;
     }
-    if (dgt0(own.y) && own.y < 1.0) {  // R- = nm / dm
-      const double r = 1.0 / dm, q = lrm * r;
-      lmnv = -q, lup += q, ldm = -q * nm * r;
+    if (dgt0(own.y) && dkey(own.y) < kOne) {  // R- = (up - min) / (-dthi flxOut + eps)
+      const double dm = fma(-dthi, fo, eps), r = rcp_nr(dm), q = lrm * r;
+      lb.y = -q, lup += q, ldm = -q * (up - mn) * r;
     }
-    a.lfi[it] = ldp * dthi;
-    a.lfo[it] = -ldm * dthi;
+    a.lfio[it] = make_double2(ldp * dthi, -ldm * dthi);
     a.ltrs[it] = lup * hin * hpi;
     a.ltl[it] = lup * dthi;
-    a.lmx[it] = lmxv, a.amx[it] = cmx;
-    a.lmn[it] = lmnv, a.amn[it] = cmn;
+    a.lmm[it] = lb;
+    a.amm[it] = make_int2(smx < 0 ? c : m.coc[(int64_t)smx * m.nC + c], smn < 0 ? c : m.coc[(int64_t)smn * m.nC + c]);
     lh = fma(lup * trc, hpi, lh);
     lhpi = fma(lup, num, lhpi);
     lhpi = fma(fma(ldp, fi, -ldm * fo), dtia, lhpi);
   }
+  if (lane) return;
   // hProv = h + dt tend_h: its cotangent goes to h and to the thickness tendency
   const double lhp = -lhpi * hpi * hpi;
   a.muh_t[i] = lh + lhp;
@@ -398,13 +430,15 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
 
 // TB (edges): the cotangents of the stage's edge fluxes.  FCT: the limited
 // antidiffusive flux A' and the cell sums (tLO, flxIn, flxOut) give A and LO;
-// LO = dv F tr_upwind and HO = F sum_a w_a tr_a (or the centred flux where the
-// high-order mask is 0) give F and the tracers (solve.cc:99-167, 216-229).
+// LO = dv F tr_upwind and HO = F S (S the advection-stencil sum of the
+// tracer, or dv (tr1 + tr2) / 2 where the high-order mask is 0) give F and
+// the tracers (solve.cc:99-167, 216-229).  S is read back as HO / F = (A +
+// LO) / F from the taped fluxes (the stencil is summed only where F = 0).
 // Without FCT: the centred flux of apps/sw/tasks/solve.cc:237-270.  del2
 // mixing (ocean solve.cc:328-366) adds to h_e and the tracers.  Per edge and
-// tracer, the parts for cells(e) go to p12 and lambda_HO F to lhof (TC
-// gathers them); per edge, the thickness-flux and edge-thickness cotangents
-// summed over tracers go to lFt / lhet (B1 adds them).
+// tracer the parts for cells(e) go to p12 and lambda_HO F, split by the sign
+// of F, to lho (TC gathers them); per edge the thickness-flux and
+// edge-thickness cotangents summed over tracers go to lFt / lhet (B1 adds them).
 __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
@@ -412,26 +446,25 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
   const int2 c = m.coe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
   const double he = 0.5 * (a.h[i1] + a.h[i2]), F = a.u[i] * he, dv = m.dvEdge[e];
-  a.Ft[i] = F;
-  const double ia1 = m.invAreaCell[c.x], ia2 = m.invAreaCell[c.y];
   const bool pos = dgt0(F), neg = dlt0(F);
   const int mask = a.fct ? m.hoMask[(int64_t)e * m.fctLev + k] : 0;
   const double kd = a.hmix ? a.kd[e] : 0.0;
+  const double rF = (pos || neg) ? rcp_nr(F) : 0.0;
   double lF = 0.0, lhe = 0.0;
   for (int t = 0; t < T; ++t) {
     const int64_t i1t = i1 * T + t, i2t = i2 * T + t, it = i * T + t;
     const double tr1 = a.tr[i1t], tr2 = a.tr[i2t];
-    const double G = a.lk_q[i2t] * ia2 - a.lk_q[i1t] * ia1;
+    const double G = a.gq[i2t] - a.gq[i1t];
     double p1 = 0.0, p2 = 0.0;
     if (a.fct) {
-      const double aa = a.A[it];
+      const double aa = a.A[it], lo = a.LO[it];
       double lA = 0.0;
       if (dgt0(aa)) {
         const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
-        lA = fma(G, r2.x < r1.y ? r2.x : r1.y, a.lfi[i2t] - a.lfo[i1t]);
+        lA = fma(G, dmin(r1.y, r2.x), a.lfio[i2t].x - a.lfio[i1t].y);
       } else if (dlt0(aa)) {
         const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
-        lA = fma(G, r2.y < r1.x ? r2.y : r1.x, a.lfo[i2t] - a.lfi[i1t]);
+        lA = fma(G, dmin(r1.x, r2.y), a.lfio[i2t].y - a.lfio[i1t].x);
       }
       const double lLO = G + (a.ltl[i2t] - a.ltl[i1t]) - lA;
       if (pos) {
@@ -441,21 +474,26 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
         lF = fma(lLO * dv, tr2, lF);
         p2 = lLO * dv * F;
       }
-      if (mask) {
-        double S = 0.0;
+      double S;
+      if (pos || neg) {
+        S = (aa + lo) * rF;
+      } else if (mask) {  // F = 0: the stencil with the centred coefficients
+        S = 0.0;
         for (int sl = 0; sl < m.nAdv[e]; ++sl) {
           const int64_t sa = (int64_t)sl * m.nE + e;
-          const double w = neg ? m.advCm[sa] : (pos ? m.advCp[sa] : m.advCoef[sa]);
-          S = fma(w, a.tr[((int64_t)m.advCells[sa] * L + k) * T + t], S);
+          S = fma(m.advCoef[sa], a.tr[((int64_t)m.advCells[sa] * L + k) * T + t], S);
         }
-        lF = fma(lA, S, lF);
-        a.lhof[it] = lA * F;
       } else {
-        const double hd = 0.5 * dv;
-        lF = fma(lA * hd, tr1 + tr2, lF);
-        const double q = lA * hd * F;
+        S = 0.5 * dv * (tr1 + tr2);
+      }
+      lF = fma(lA, S, lF);
+      const double lAF = lA * F;
+      if (mask) {
+        a.lho[it] = make_double2(pos ? lAF : 0.0, neg ? lAF : 0.0);
+      } else {
+        const double q = 0.5 * dv * lAF;
         p1 += q, p2 += q;
-        a.lhof[it] = 0.0;
+        a.lho[it] = make_double2(0.0, 0.0);
       }
     } else {
       const double hd = 0.5 * dv;
@@ -475,51 +513,72 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
 
 // TC (cells): the tracer cotangent of the stage input, gathered from the
 // upwind value, the edges of the cell, the advection stencils that read it
-// (DMesh::advR) and the bounds it holds for itself and its neighbours; then
-// q = h tr is converted and the RK bookkeeping of q runs.
+// (DMesh::advRe / advRc) and the bounds it holds for itself and its distinct
+// neighbours (DMesh::cocU); then q = h tr is converted and the RK bookkeeping
+// of q runs (g = lk_q / areaCell for the next stage beside it).  NL lanes per
+// cell split the gathers and sum by shuffles.
+template <int NL>
 __global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= (int64_t)m.nC * L) return;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int lane = (int)(g & (NL - 1));
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (g / NL >= nCL) return;  // whole groups: all lanes of a live cell stay
+  const int64_t i = g / NL;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c], T = a.T;
-  const double hinv = 1.0 / a.h[i];
+  const double hinv = rcp_nr(a.h[i]), inva = m.invAreaCell[c];
   double mh = a.fct ? a.muh_t[i] : 0.0;
   for (int t = 0; t < T; ++t) {
     const int64_t it = i * T + t;
     double lt = 0.0;
-    for (int j = 0; j < n; ++j) {
+    for (int j = lane; j < n; j += NL) {
       const int64_t s = (int64_t)j * m.nC + c;
       const double2 p = a.p12[((int64_t)m.eoc[s] * L + k) * T + t];
       lt += (m.nbr[s] & 1) ? p.x : p.y;
+      if (a.fct) {
+        const int oc = m.cocU[s];
+        if (oc >= 0) {
+          const int64_t ot = ((int64_t)oc * L + k) * T + t;
+          const int2 ao = a.amm[ot];
+          if (ao.x == c) lt += a.lmm[ot].x;
+          if (ao.y == c) lt += a.lmm[ot].y;
+        }
+      }
     }
+    if (a.fct)
+      for (int j0 = lane; j0 < m.maxAdvR; j0 += 4 * NL) {
+        // four entries per lane in flight: indices first, then the gathers
+        int e[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = j0 + u * NL;
+          e[u] = j < m.maxAdvR ? m.advRe[(int64_t)j * m.nC + c] : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (e[u] < 0) continue;
+          // one of {F > 0 part, F < 0 part} is +0: pick the other with its coefficient
+          const double2 w = m.advRc[(int64_t)(j0 + u * NL) * m.nC + c];
+          const double2 l = a.lho[((int64_t)e[u] * L + k) * T + t];
+          const bool p = dbits(l.x) != 0;
+          lt = fma(p ? w.x : w.y, p ? l.x : l.y, lt);
+        }
+        if (e[3] < 0) break;
+      }
+    lt = lane_sum<NL>(lt);
+    if (lane) continue;
     if (a.fct) {
       lt += a.ltrs[it];
-      if (a.amx[it] == c) lt += a.lmx[it];
-      if (a.amn[it] == c) lt += a.lmn[it];
-      for (int j = 0; j < n; ++j) {  // each distinct neighbour once
-        const int oc = m.coc[(int64_t)j * m.nC + c];
-        bool dup = oc == c;
-        for (int p = 0; p < j && !dup; ++p) dup = m.coc[(int64_t)p * m.nC + c] == oc;
-        if (dup) continue;
-        const int64_t ot = ((int64_t)oc * L + k) * T + t;
-        if (a.amx[ot] == c) lt += a.lmx[ot];
-        if (a.amn[ot] == c) lt += a.lmn[ot];
-      }
-      for (int j = 0; j < m.maxAdvR; ++j) {
-        const int v = m.advR[(int64_t)j * m.nC + c];
-        if (v < 0) break;
-        const int e = v >> 4;
-        const int64_t sa = (int64_t)(v & 15) * m.nE + e, ie = (int64_t)e * L + k;
-        const double F = a.Ft[ie];
-        const double w = dlt0(F) ? m.advCm[sa] : (dgt0(F) ? m.advCp[sa] : m.advCoef[sa]);
-        lt = fma(w, a.lhof[ie * T + t], lt);
-      }
+      const int2 am = a.amm[it];
+      const double2 lb = a.lmm[it];
+      if (am.x == c) lt += lb.x;
+      if (am.y == c) lt += lb.y;
     }
     const double mq = lt * hinv;  // tr = q / h
     mh = fma(-mq, a.tr[it], mh);
-    combine(a.rk, a.dt, it, mq, a.lam_q, a.acc_q, a.lk_q);
+    a.gq[it] = combine(a.rk, a.dt, it, mq, a.lam_q, a.acc_q, a.lk_q) * inva;
   }
-  a.muh_t[i] = mh;
+  if (lane == 0) a.muh_t[i] = mh;
 }
 
 // Window ends: lambda_q = lambda_tr / h, lambda_h -= sum_t lambda_tr tr / h
@@ -542,6 +601,15 @@ __global__ void k_adj_q_convert(int64_t nCL, int T, const double *h, const doubl
     }
   }
   lam_h[i] = lh;
+}
+
+// lk_q = c lam_q and g = lk_q / areaCell
+__global__ void k_adj_init_q(DMesh m, int L, int T, const double *lam, double *lk, double *g, double c) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nC * L * T) return;
+  const double l = c * lam[i];
+  lk[i] = l;
+  g[i] = l * m.invAreaCell[i / ((int64_t)L * T)];
 }
 
 __global__ void k_adj_init(int64_t n, const double *lam, double *lk, double c) {
@@ -568,11 +636,11 @@ void ensure_buffers(SwState &s, int N, int k) {
     const int64_t cT = ch * s.T, eT = eu * s.T;
     const std::vector<std::pair<double **, int64_t>> tb = {
         {&A->ck_tr, nck * cT}, {&A->tp_tr, (4LL * k + 1) * cT}, {&A->tp_A, 4LL * k * eT},
-        {&A->tp_LO, 4LL * k * eT}, {(double **)&A->tp_R2, 8LL * k * cT}, {&A->trhacc, cT},
-        {&A->lam_q, cT}, {&A->acc_q, cT}, {&A->lk_q, cT}, {&A->ltl, cT}, {&A->lfi, cT}, {&A->lfo, cT},
-        {&A->lmx, cT}, {&A->lmn, cT}, {&A->ltrs, cT}, {(double **)&A->amx, (cT + 1) / 2},
-        {(double **)&A->amn, (cT + 1) / 2}, {&A->muh_t, ch}, {&A->lFt, eu}, {&A->lhet, eu}, {&A->Ft, eu},
-        {&A->lhof, eT}, {(double **)&A->p12, 2 * eT}};
+        {&A->tp_LO, 4LL * k * eT}, {(double **)&A->tp_R2, 8LL * k * cT}, {&A->tp_tLO, 4LL * k * cT},
+        {&A->tp_hpi, 4LL * k * ch}, {&A->trhacc, cT}, {&A->lam_q, cT}, {&A->acc_q, cT}, {&A->lk_q, cT},
+        {&A->gq, cT}, {&A->ltl, cT}, {&A->ltrs, cT}, {(double **)&A->lfio, 2 * cT},
+        {(double **)&A->lmm, 2 * cT}, {(double **)&A->amm, cT}, {&A->muh_t, ch}, {&A->lFt, eu},
+        {&A->lhet, eu}, {(double **)&A->lho, 2 * eT}, {(double **)&A->p12, 2 * eT}};
     bufs.insert(bufs.end(), tb.begin(), tb.end());
   }
   size_t total = 0;
@@ -620,14 +688,20 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
     TrArgs t{};
     t.u = a.u, t.h = a.h, t.tr = A.tp_tr + (size_t)j * cT;
     t.A = A.tp_A + (size_t)j * eT, t.LO = A.tp_LO + (size_t)j * eT, t.R2 = A.tp_R2 + (size_t)j * cT;
-    t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
-    t.ltl = A.ltl, t.lfi = A.lfi, t.lfo = A.lfo, t.lmx = A.lmx, t.lmn = A.lmn, t.ltrs = A.ltrs;
-    t.amx = A.amx, t.amn = A.amn, t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.Ft = A.Ft;
-    t.lhof = A.lhof, t.p12 = A.p12;
+    t.hpi = A.tp_hpi + (size_t)j * nC, t.tLO = A.tp_tLO + (size_t)j * cT;
+    t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.gq = A.gq, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
+    t.ltl = A.ltl, t.ltrs = A.ltrs, t.lfio = A.lfio, t.lmm = A.lmm, t.amm = A.amm;
+    t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.p12 = A.p12, t.lho = A.lho;
     t.T = s.T, t.rk = rk, t.fct = s.p.fct ? 1 : 0, t.hmix = s.p.hmix ? 1 : 0, t.dt = A.dt;
-    if (t.fct) launch_pdl(k_adj_tr_a, nC, TPB, pdl, st, m, t, L);
+    constexpr int NLA = 1, NLC = 2;  // lanes per cell (measured best at level 6)
+    if (t.fct) {
+      if (m.maxEoC <= 6)
+        launch_pdl(k_adj_tr_a<NLA, 6>, nC * NLA, TPB, pdl, st, m, t, L);
+      else
+        launch_pdl(k_adj_tr_a<NLA, 0>, nC * NLA, TPB, pdl, st, m, t, L);
+    }
     launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
-    launch_pdl(k_adj_tr_c, nC, TPB, pdl, st, m, t, L);
+    launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
     a.lFt = A.lFt, a.lhet = A.lhet, a.muh_t = A.muh_t;
   }
   if (m.maxEoE == 10)
@@ -705,6 +779,7 @@ void reverse_body(SwState &s) {
         S.u_new = rk == 3 ? ou : nullptr, S.h_new = rk == 3 ? oh : nullptr;
         S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
         S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
+        S.tLO = A.tp_tLO + (size_t)j * cT, S.tape_hpi = A.tp_hpi + (size_t)j * ch;
         S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next;
         sw_launch_stage(s, S, st);
       }
@@ -717,7 +792,8 @@ void reverse_body(SwState &s) {
                                                               A.tp_tr + (size_t)4 * n * cT, A.lam_q, A.lam_h, 0);
       k_adj_init<<<blocks_for(eu, TPB), TPB, 0, st>>>(eu, A.lam_u, A.lk_u, A.dt / 6);
       k_adj_init<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, A.lam_h, A.lk_h, A.dt / 6);
-      if (A.tr) k_adj_init<<<blocks_for(cT, TPB), TPB, 0, st>>>(cT, A.lam_q, A.lk_q, A.dt / 6);
+      if (A.tr)
+        k_adj_init_q<<<blocks_for(cT, TPB), TPB, 0, st>>>(m, s.L, s.T, A.lam_q, A.lk_q, A.gq, A.dt / 6);
     }
     for (int t = n - 1; t >= 0; --t)
       for (int rk = 3; rk >= 0; --rk) {

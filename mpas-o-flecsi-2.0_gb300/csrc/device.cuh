@@ -71,10 +71,13 @@ struct DMesh {
   const double *woeT;         // [maxEoE][nE] weight of e in the stencil of eoe[j][e] (0 in pads)
   const int *vocR;            // [maxEoC][nC] vertices of c (pads repeat slot 0)
   const double *kiteR;        // [maxEoC][nC] kite of c at vocR[j][c] (0 in pads)
-  // [maxAdvR][nC] (edge << 4) | slot of every advection stencil entry that
-  // reads the cell (advCells[slot][edge] == c), ascending edge, -1 pads last
-  const int *advR;
+  // [maxAdvR][nC] every advection stencil entry that reads the cell
+  // (advCells[slot][edge] == c): the edge (ascending, -1 pads last) and the
+  // cell's coefficient pair there {advCp, advCm}
+  const int *advRe;
+  const double2 *advRc;
   int maxAdvR;
+  const int *cocU;            // [maxEoC][nC] cellsOnCell, -1 for the cell itself and repeats
 };
 
 // Host-side mesh context.

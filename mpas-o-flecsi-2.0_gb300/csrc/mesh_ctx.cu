@@ -343,18 +343,34 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   for (int64_t c = 0; c < nC; ++c)
     for (int j = fillc[c]; j < maxEoC; ++j) vocR[(size_t)j * nC + c] = vocR[c];
   A.add(woeT, &m.woeT), A.add(vocR, &m.vocR), A.add(kiteR, &m.kiteR);
-  // cell -> (edge, slot) entries of the advection stencils that read the cell,
-  // (edge << 4) | slot, ascending edge; -1 pads at the end of each column
+  // cell -> entries of the advection stencils that read the cell: the edge
+  // (ascending; -1 pads at the end of each column) and the coefficient pair
+  // {advCoef + 0.25 advCoef_3rd, advCoef - 0.25 advCoef_3rd} of the cell there
   std::vector<std::vector<int>> rev(ctx.has_fct ? nC : 0);
   for (int64_t k = 0; ctx.has_fct && k < nE; ++k)
-    for (int j = 0; j < nAdv[k]; ++j) rev[advCells[(size_t)j * nE + k]].push_back((int)(k << 4) | j);
+    for (int j = 0; j < nAdv[k]; ++j) rev[advCells[(size_t)j * nE + k]].push_back((int)(j * nE + k));
   int maxAdvR = 1;
   for (auto &r : rev) maxAdvR = std::max(maxAdvR, (int)r.size());
-  std::vector<int> advR((size_t)maxAdvR * nC, -1);
+  std::vector<int> advRe((size_t)maxAdvR * nC, -1);
+  std::vector<double> advRc((size_t)2 * maxAdvR * nC, 0.0);
   for (size_t c = 0; c < rev.size(); ++c)
-    for (size_t j = 0; j < rev[c].size(); ++j) advR[j * nC + c] = rev[c][j];
+    for (size_t j = 0; j < rev[c].size(); ++j) {
+      const size_t sa = (size_t)rev[c][j], o = j * nC + c;
+      advRe[o] = (int)(sa % (size_t)nE);
+      advRc[2 * o] = cp[sa], advRc[2 * o + 1] = cm[sa];
+    }
   m.maxAdvR = maxAdvR;
-  A.add(advR, &m.advR);
+  A.add(advRe, &m.advRe), A.add(advRc, (const double **)&m.advRc);
+  // cellsOnCell with the cell itself and repeated neighbours replaced by -1
+  std::vector<int> cocU((size_t)maxEoC * nC, -1);
+  for (int64_t c = 0; c < nC; ++c)
+    for (int j = 0; j < nEoC[c]; ++j) {
+      const int o = coc[(size_t)j * nC + c];
+      bool dup = o == (int)c;
+      for (int p = 0; p < j && !dup; ++p) dup = coc[(size_t)p * nC + c] == o;
+      if (!dup) cocU[(size_t)j * nC + c] = o;
+    }
+  A.add(cocU, &m.cocU);
 
   A.upload(ctx);
   ctx.perm[0] = pc, ctx.perm[1] = pe, ctx.perm[2] = pv;

@@ -138,6 +138,7 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
     // provisional thickness (apps/ocean/tasks/solve.cc:60-97): h + dt tend_h
     const double hin = S.h_in[i];
     const double hpi = S.fct ? rcp_nr(fma(S.dt, tend_h, hin)) : 0.0;
+    if (S.tape_hpi) S.tape_hpi[i] = hpi;
     if constexpr (SPLIT)
       S.hpw[i] = hpi;
     else

@@ -94,6 +94,7 @@ struct Stage {
   double *tLO;                              // cell intermediates
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
   double *tape_pv, *tape_hs;                // adjoint taping: pv and kite-summed h of the next state
+  double *tape_hpi;                         // adjoint taping: 1/hProv of the stage (FCT)
   double *hpw;                              // sw four-launch schedule: 1/hProv from K2 to the limiter
 };
 
