@@ -209,6 +209,12 @@ typedef struct {
 #define MPASO_FIELD_U 1                    /* sw u / ocean normalVelocity [nE][L] */
 #define MPASO_FIELD_TRACERS 2              /* [nC][L][T] */
 #define MPASO_FIELD_LAYER_THICKNESS_EDGE 3 /* ocean layerThicknessEdge [nE][L] */
+/* sw diagnostics of the current state, read-only (get / snapshot): the
+ * vorticity and pv_vertex fields compute_solve_diagnostics produces
+ * (apps/sw/tasks/solve.cc:56-60, 90) and the sw history output writes as
+ * "vorticity" / "potential_vorticity" (mpasoflecsi/io/desc.hh:46-56) */
+#define MPASO_FIELD_VORTICITY 4            /* [nV][L] */
+#define MPASO_FIELD_PV_VERTEX 5            /* [nV][L] */
 
 int mpaso_state_create(mpaso_mesh m, const mpaso_params *p, mpaso_state *out);
 int mpaso_state_destroy(mpaso_state s);

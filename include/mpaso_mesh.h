@@ -35,6 +35,7 @@ extern "C" {
 #define MPASO_ERR_TIMEOUT 6   /* a bounded device-side wait gave up */
 #define MPASO_ERR_NUMERIC 7   /* non-finite value detected where checked */
 #define MPASO_ERR_NODEVICE 8  /* no CUDA device available */
+#define MPASO_ERR_IO 9        /* file open / read / write failure or malformed file */
 
 #define MPASO_DTYPE_INT32 0
 #define MPASO_DTYPE_FLOAT64 1

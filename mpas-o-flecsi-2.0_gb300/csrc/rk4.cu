@@ -607,6 +607,12 @@ void field_geom(SwState &s, int field, int &entity, int64_t &row, double *&buf) 
       require(s.p.app == MPASO_APP_OCEAN, MPASO_ERR_ARG, "layerThicknessEdge is an ocean field");
       entity = MPASO_EDGES, row = s.L, buf = s.HE;
       break;
+    case MPASO_FIELD_VORTICITY:
+    case MPASO_FIELD_PV_VERTEX:
+      require(s.p.app == MPASO_APP_SW, MPASO_ERR_ARG, "vorticity / pv_vertex are sw diagnostics");
+      ensure_diag(s, s.stream);  // diagnostics of the current state (kept current by the steps)
+      entity = MPASO_VERTICES, row = s.L, buf = field == MPASO_FIELD_VORTICITY ? s.vort : s.pv;
+      break;
     default: fail(MPASO_ERR_ARG, "unknown field id");
   }
   require(row > 0, MPASO_ERR_ARG, "field has no data (ntr = 0?)");
@@ -833,6 +839,8 @@ int mpaso_state_set(mpaso_state s, int32_t field, const double *data) {
     require(s && data, MPASO_ERR_ARG, "null argument");
     SwState &S = s->s;
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    require(field != MPASO_FIELD_VORTICITY && field != MPASO_FIELD_PV_VERTEX, MPASO_ERR_ARG,
+            "diagnostic fields are read-only");
     int entity;
     int64_t row;
     double *buf;

@@ -18,6 +18,7 @@ _lp = ctypes.POINTER(ctypes.c_int64)
 CELLS, EDGES, VERTICES = 0, 1, 2
 APP_SW, APP_OCEAN = 0, 1
 FIELD_H, FIELD_U, FIELD_TRACERS, FIELD_LAYER_THICKNESS_EDGE = 0, 1, 2, 3
+FIELD_VORTICITY, FIELD_PV_VERTEX = 4, 5  # sw diagnostics of the current state, read-only
 
 
 class MeshDesc(ctypes.Structure):
@@ -236,7 +237,8 @@ class State:
         dm = self.dmesh
         return {FIELD_H: (dm.nC, self.L), FIELD_U: (dm.nE, self.L),
                 FIELD_TRACERS: (dm.nC, self.L, self.T),
-                FIELD_LAYER_THICKNESS_EDGE: (dm.nE, self.L)}[field]
+                FIELD_LAYER_THICKNESS_EDGE: (dm.nE, self.L), FIELD_VORTICITY: (dm.nV, self.L),
+                FIELD_PV_VERTEX: (dm.nV, self.L)}[field]
 
     def set(self, field, data):
         if isinstance(data, np.ndarray):
