@@ -9,6 +9,15 @@
   rotated by the elapsed time (apps/sw/tasks/solve.cc:404-436); its ctest
   (apps/sw/CMakeLists.txt:28-31, 5 steps of the default dt = 40 s on a
   240 km quasi-uniform sphere) requires <= 0.0015 (apps/sw/finalize.cc:24-25).
+- `ocean_case`, `ocean_case_error`: the ocean app's three test cases
+  (apps/ocean/tasks/testcase.cc:16-173) -- a Gaussian hill (1) and a slotted
+  cylinder (2) carried once round the sphere in a day by solid-body rotation
+  with unit thickness (FCT advection), and a spherical harmonic of degree 2
+  (3) decaying under del2 mixing at exp(-6 kappa t / a^2) -- with their error
+  norms (:175-294): the root of the summed squared pointwise relative errors
+  over nCells, and the largest relative error.  (The reference's running
+  maximum compares |error| with a signed value, so it can report a smaller
+  one; the true maximum is returned here.)
 - `del2_mode`: a divergence-free planar Fourier mode u = curl(A sin(2 pi x /
   Lx)) on an f = 0 doubly periodic mesh with uniform h, whose only dynamics at
   small amplitude is viscous decay exp(-nu k^2 t) (k = 2 pi / Lx): the known
@@ -66,3 +75,76 @@ def del2_mode(mesh, amp=1e-6, h0=1000.0):
     u = amp * pattern
     h = np.full((mesh.nCells, 1), h0)
     return h, u[:, None].copy(), pattern, k * k
+
+
+# ---------------------------------------------------------------- ocean app
+_DAY = 86400.0
+
+
+def ocean_rotation_velocity(mesh, a=EARTH_RADIUS):
+    """Normal velocity of solid-body rotation with a one-day period
+    (apps/ocean/tasks/testcase.cc:16-22): u0 cos(latEdge) cos(angleEdge)."""
+    f = mesh.fields
+    u0 = 2.0 * np.pi * a / _DAY
+    return u0 * np.cos(f["latEdge"]) * np.cos(f["angleEdge"])
+
+
+def _gaussian(x, a):
+    maxg = 21983.7698959881  # :28-31
+    return 50.0 + (20.0 / maxg) * np.exp(10.0 * x / a)
+
+
+def _slotted_cylinder(x, y, z, lat, lon, a):
+    """apps/ocean/tasks/testcase.cc:36-60 (arc length as mpasoflecsi/eqns/metrics.hh:75-90)."""
+    r = np.sqrt(x * x + y * y + z * z)
+    c = np.sqrt((a - x) ** 2 + y ** 2 + z ** 2)
+    dist = r * 2.0 * np.arcsin(c / (2.0 * r))
+    lon = np.where(lon > np.pi, lon - 2.0 * np.pi, lon)
+    slot = (a * lat > -a / 3.0) & (a * lat < a / 2.0) & (a * np.abs(lon) < a / 12.0)
+    return np.where(dist > a / 2.0, 50.0, np.where(slot, 50.0, 100.0))
+
+
+def _harmonic(lat, lon, coef, t, a):
+    """apps/ocean/tasks/testcase.cc:62-73."""
+    return 50.0 + 20.0 * np.cos(lat) ** 2 * np.cos(2.0 * lon) * np.exp(-6.0 * coef * t / (a * a))
+
+
+def ocean_case(mesh, case, coef=1e7, a=EARTH_RADIUS):
+    """(h [nC][1], u [nE][1], tracers [nC][1][1]) of ocean test case 1, 2 or 3
+    (setup_case_1/2/3, apps/ocean/tasks/testcase.cc:96-173); case 3 is at rest."""
+    f = mesh.fields
+    h = np.ones((mesh.nCells, 1))
+    u = ocean_rotation_velocity(mesh, a)[:, None] if case in (1, 2) else np.zeros((mesh.nEdges, 1))
+    if case == 1:
+        tr = _gaussian(f["xCell"], a)
+    elif case == 2:
+        tr = _slotted_cylinder(f["xCell"], f["yCell"], f["zCell"], f["latCell"], f["lonCell"], a)
+    elif case == 3:
+        tr = _harmonic(f["latCell"], f["lonCell"], coef, 0.0, a)
+    else:
+        raise ValueError("ocean test cases are 1, 2 and 3")
+    return h, u, np.ascontiguousarray(tr[:, None, None])
+
+
+def ocean_case_exact(mesh, case, elapsed, coef=1e7, a=EARTH_RADIUS):
+    """The analytic tracer of case 1, 2 or 3 after `elapsed` seconds
+    (calc_error_case_1/2/3, apps/ocean/tasks/testcase.cc:175-294)."""
+    f = mesh.fields
+    rot = 2.0 * np.pi * elapsed / _DAY
+    x, y = f["xCell"], f["yCell"]
+    if case == 1:
+        return _gaussian(x * np.cos(-rot) - y * np.sin(-rot), a)
+    if case == 2:
+        xp = x * np.cos(rot) + y * np.sin(rot)
+        yp = -x * np.sin(rot) + y * np.cos(rot)
+        return _slotted_cylinder(xp, yp, f["zCell"], f["latCell"], f["lonCell"] - rot, a)
+    return _harmonic(f["latCell"], f["lonCell"], coef, elapsed, a)
+
+
+def ocean_case_error(mesh, case, tracers, elapsed, coef=1e7, a=EARTH_RADIUS):
+    """(l2, max) of the pointwise relative error of tracer 0, level 0, against the
+    analytic solution: l2 = sqrt(sum err^2) / nCells as the reference reports it."""
+    tr = np.asarray(tracers).reshape(mesh.nCells, -1)[:, 0]
+    exact = ocean_case_exact(mesh, case, elapsed, coef, a)
+    err = (tr - exact) / exact
+    return float(np.sqrt(np.sum(err * err)) / mesh.nCells), float(np.abs(err).max())

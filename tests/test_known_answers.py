@@ -4,8 +4,26 @@ tests/test_gpu_rk4.py."""
 import numpy as np
 
 import mpaso
-from mpaso.testcases import del2_mode, sw_case1, sw_case1_error
+from mpaso.setup import fct_statics
+from mpaso.testcases import del2_mode, ocean_case, ocean_case_error, sw_case1, sw_case1_error
 from oracle import Oracle
+
+# ocean test cases (apps/ocean/tasks/testcase.cc): (dt, days) per icosahedral level
+OCEAN_RUN = {1: {3: (1800.0, 1), 4: (900.0, 1)}, 2: {4: (900.0, 1)}, 3: {4: (3600.0, 10), 5: (1800.0, 10)}}
+
+
+def ocean_run(level, case):
+    """The ocean app (apps/ocean/run.cc:10-50) on test case `case` with the oracle;
+    FCT advection for the rotating cases, del2 mixing (kappa = 1e7, as
+    apps/ocean/initialize.cc:79 sets) for the diffusing one."""
+    S = Oracle("restatement")
+    m = mpaso.Mesh.icosa(level)
+    h, u, tr = ocean_case(m, case)
+    dt, days = OCEAN_RUN[case][level]
+    n = int(round(days * 86400.0 / dt))
+    cfg = S.config(1, 1, fct=True) if case in (1, 2) else S.config(1, 1, hmix=True, kappa=1e7)
+    out = S.ocean_run(m, S.static(m, fct_statics(m, 1)), cfg, dt, n, h, np.ones((m.nEdges, 1)), u, tr)
+    return m, tr, out, n * dt
 
 
 def test_sw_case1_error_within_reference_tolerance():
@@ -34,3 +52,37 @@ def test_del2_momentum_decays_a_fourier_mode_at_nu_k2():
     # dissipative: with nu = 0 the mode keeps its amplitude
     _, u0, _ = S.sw_run(m, S.static(m), S.config(1, 0, nu=0.0), dt, n, h, u, np.zeros((m.nCells, 1, 0)))
     assert abs(float((u0[:, 0] * pattern).sum() / (pattern * pattern).sum()) / 1e-6 - 1) < 1e-6
+
+
+def test_ocean_case3_diffusion_decays_at_6_kappa_over_a2():
+    """Ocean case 3: a degree-2 spherical harmonic under del2 mixing decays as
+    exp(-6 kappa t / a^2); after 10 days the pointwise relative error is 3e-4
+    at level 4 and falls ~4x per level (second order), the l2 norm ~8x."""
+    m4, _, out4, t4 = ocean_run(4, 3)
+    l2_4, mx4 = ocean_case_error(m4, 3, out4, t4)
+    m5, _, out5, t5 = ocean_run(5, 3)
+    l2_5, mx5 = ocean_case_error(m5, 3, out5, t5)
+    assert l2_4 < 4e-6 and mx4 < 4e-4
+    assert mx5 < 0.3 * mx4 and l2_5 < 0.2 * l2_4
+
+
+def test_ocean_case1_gaussian_hill_one_rotation():
+    """Ocean case 1: a Gaussian hill carried once round the sphere by FCT advection
+    comes back with a relative l2 error that shrinks with resolution, no overshoot
+    of its initial maximum and an undershoot of the background below 0.05%."""
+    errs = {}
+    for level in (3, 4):
+        m, tr0, out, t = ocean_run(level, 1)
+        errs[level] = ocean_case_error(m, 1, out, t)[0]
+        assert out.max() <= tr0.max() and out.min() > 50.0 * (1 - 2e-3)
+    assert errs[4] < 5e-4 and errs[4] < 0.5 * errs[3]
+
+
+def test_ocean_case2_slotted_cylinder_stays_in_range():
+    """Ocean case 2: the slotted cylinder (values 50 and 100) after one rotation:
+    the FCT limiter keeps it inside [50, 100] up to a 0.2% undershoot of the
+    background (the prescribed unit thickness is not the provisional thickness
+    the limiter bounds against), and the l2 error stays below 2.5e-3."""
+    m, tr0, out, t = ocean_run(4, 2)
+    assert out.max() <= 100.0 and out.min() > 50.0 * (1 - 2e-3)
+    assert ocean_case_error(m, 2, out, t)[0] < 2.5e-3
