@@ -9,6 +9,11 @@
   rotated by the elapsed time (apps/sw/tasks/solve.cc:404-436); its ctest
   (apps/sw/CMakeLists.txt:28-31, 5 steps of the default dt = 40 s on a
   240 km quasi-uniform sphere) requires <= 0.0015 (apps/sw/finalize.cc:24-25).
+- `sw_case5`, `sw_case6`: Williamson cases 5 (zonal flow over an isolated
+  mountain, with the reference's two cone tracers) and 6 (Rossby-Haurwitz wave
+  of wavenumber 4), as apps/sw/tasks/testcase.cc:80-227 sets them up; the
+  reference runs them as stability runs, and `sw_invariants` gives the
+  discrete mass, tracer mass and energy whose conservation the tests check.
 - `ocean_case`, `ocean_case_error`: the ocean app's three test cases
   (apps/ocean/tasks/testcase.cc:16-173) -- a Gaussian hill (1) and a slotted
   cylinder (2) carried once round the sphere in a day by solid-body rotation
@@ -25,7 +30,9 @@
 """
 import numpy as np
 
-from .mesh import EARTH_RADIUS
+from .mesh import EARTH_RADIUS, OMEGA
+
+GRAVITY = 9.80616  # mpasoflecsi/common/constants.hh:30-31
 
 
 def sphere_distance(lat1, lon1, lat2, lon2, radius):
@@ -63,6 +70,68 @@ def sw_case1_error(mesh, h, elapsed, a=EARTH_RADIUS):
     num = np.sum((np.asarray(h).reshape(mesh.nCells, -1)[:, 0] - ht) ** 2 * w) / (4 * np.pi)
     den = np.sum(ht ** 2 * w) / (4 * np.pi)
     return float(np.sqrt(num) / np.sqrt(den))
+
+
+def _psi_to_u(mesh, psi_vertex):
+    """Normal velocity of a streamfunction at vertices, as the reference builds it."""
+    v = mesh.fields["verticesOnEdge"] - 1
+    return -(psi_vertex[v[:, 1]] - psi_vertex[v[:, 0]]) / mesh.fields["dvEdge"]
+
+
+def sw_case5(mesh, a=EARTH_RADIUS, omega=OMEGA, g=GRAVITY):
+    """(h [nC][1], u [nE][1], h_s [nC], tracers [nC][1][2]) of Williamson case 5
+    (apps/sw/tasks/testcase.cc:80-168): alpha = 0, so f keeps its usual form."""
+    f = mesh.fields
+    u0, gh0, hs0 = 20.0, 5960.0 * g, 2000.0
+    theta_c, lambda_c, rr = np.pi / 6.0, 3.0 * np.pi / 2.0, np.pi / 9.0
+    u = _psi_to_u(mesh, -a * u0 * np.sin(f["latVertex"]))
+    lat, lon = f["latCell"], np.where(f["lonCell"] < 0, f["lonCell"] + 2.0 * np.pi, f["lonCell"])
+    r = np.sqrt(np.minimum(rr ** 2, (lon - lambda_c) ** 2 + (lat - theta_c) ** 2))
+    hs = hs0 * (1.0 - r / rr)
+    r2 = np.sqrt(np.minimum(rr ** 2, (lon - lambda_c) ** 2 + (lat - theta_c - np.pi / 6.0) ** 2))
+    tr = np.stack([1.0 - r / rr, 1.0 - r2 / rr], axis=1)[:, None, :]
+    h = (gh0 - (a * omega * u0 + 0.5 * u0 ** 2) * np.sin(lat) ** 2) / g - hs
+    return h[:, None].copy(), u[:, None].copy(), hs, np.ascontiguousarray(tr)
+
+
+def sw_case6(mesh, a=EARTH_RADIUS, omega=OMEGA, g=GRAVITY):
+    """(h [nC][1], u [nE][1]) of the Rossby-Haurwitz wave, Williamson case 6
+    (apps/sw/tasks/testcase.cc:171-225)."""
+    f = mesh.fields
+    h0, w, K, R = 8000.0, 7.848e-6, 7.848e-6, 4.0
+    latv, lonv = f["latVertex"], f["lonVertex"]
+    psi = -a * a * w * np.sin(latv) + a * a * K * np.cos(latv) ** R * np.sin(latv) * np.cos(R * lonv)
+    u = _psi_to_u(mesh, psi)
+    th, lon = f["latCell"], f["lonCell"]
+    c = np.cos(th)
+    A = (0.5 * w * (2.0 * omega + w) * c ** 2 +
+         0.25 * K ** 2 * c ** (2 * R) * ((R + 1.0) * c ** 2 + 2.0 * R ** 2 - R - 2.0 - 2.0 * R ** 2 * c ** -2))
+    B = (2.0 * (omega + w) * K / ((R + 1.0) * (R + 2.0))) * c ** R * ((R ** 2 + 2.0 * R + 2.0) - ((R + 1.0) * c) ** 2)
+    C = 0.25 * K ** 2 * c ** (2.0 * R) * ((R + 1.0) * c ** 2 - R - 2.0)
+    h = (g * h0 + a * a * A + a * a * B * np.cos(R * lon) + a * a * C * np.cos(2.0 * R * lon)) / g
+    return h[:, None].copy(), u[:, None].copy()
+
+
+def sw_invariants(mesh, h, u, tracers=None, h_s=None, g=GRAVITY):
+    """Discrete mass sum(A h), tracer masses sum(A h tr) and total energy
+    sum_c A (h K + g h (h/2 + h_s)), K the cell kinetic energy of
+    compute_solve_diagnostics (apps/sw/tasks/solve.cc:62-77), level 0."""
+    f = mesh.fields
+    A = f["areaCell"]
+    hh = np.asarray(h).reshape(mesh.nCells, -1)[:, 0]
+    uu = np.asarray(u).reshape(mesh.nEdges, -1)[:, 0]
+    e = f["edgesOnCell"] - 1
+    n = f["nEdgesOnCell"]
+    valid = np.arange(e.shape[1])[None, :] < n[:, None]
+    w = (0.25 * f["dcEdge"] * f["dvEdge"])[np.where(valid, e, 0)] * valid
+    ke = (w * uu[np.where(valid, e, 0)] ** 2).sum(axis=1) / A
+    hs = np.zeros(mesh.nCells) if h_s is None else np.asarray(h_s)
+    out = {"mass": float((A * hh).sum()),
+           "energy": float((A * (hh * ke + g * hh * (0.5 * hh + hs))).sum())}
+    if tracers is not None:
+        tr = np.asarray(tracers).reshape(mesh.nCells, -1, np.asarray(tracers).shape[-1])[:, 0, :]
+        out["tracer_mass"] = (A[:, None] * hh[:, None] * tr).sum(axis=0)
+    return out
 
 
 def del2_mode(mesh, amp=1e-6, h0=1000.0):

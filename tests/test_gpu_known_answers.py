@@ -1,13 +1,14 @@
-"""The ocean app's three test cases through the CUDA path (GPU): the tracers
-after the full run agree with the oracle's run to the 100-step parity bar, and
-the analytic error norms meet the bounds the CPU known-answer tests set."""
+"""The ocean app's three test cases and sw cases 5 and 6 through the CUDA path
+(GPU): the state after the full run agrees with the oracle's run to the
+100-step parity bar, and the analytic error norms and conserved quantities meet
+the bounds the CPU known-answer tests set."""
 import numpy as np
 import pytest
 
 from helpers import rel_max
 from mpaso.setup import fct_statics
-from mpaso.testcases import ocean_case, ocean_case_error
-from test_known_answers import OCEAN_RUN, ocean_run
+from mpaso.testcases import ocean_case, ocean_case_error, sw_invariants
+from test_known_answers import OCEAN_RUN, ocean_run, sw_case_run
 
 pytestmark = pytest.mark.gpu
 
@@ -35,3 +36,26 @@ def test_ocean_case_on_device(case):
     else:
         assert got.max() <= tr0.max() and got.min() > 50.0 * (1 - 2e-3)
         assert l2 < (5e-4 if case == 1 else 2.5e-3)
+
+
+@pytest.mark.parametrize("case", [5, 6])
+def test_sw_case_on_device(case):
+    import mpaso.gpu as G
+    m, (h, u, tr, hs), want = sw_case_run(case)
+    T = 0 if case == 6 else 2
+    dm = G.DeviceMesh(m, fct=fct_statics(m, 1) if T else None, bottomDepth=hs)
+    st = G.State(dm, nlev=1, ntr=T, fct=bool(T))
+    st.set(G.FIELD_H, h)
+    st.set(G.FIELD_U, u)
+    if T:
+        st.set(G.FIELD_TRACERS, tr)
+    st.step_graph(600.0, 144)
+    got = (st.get(G.FIELD_H), st.get(G.FIELD_U)) + ((st.get(G.FIELD_TRACERS),) if T else ())
+    for a, b in zip(got, want):
+        assert rel_max(a, b) < 1e-9
+    i0 = sw_invariants(m, h, u, tr if T else None, hs)
+    i1 = sw_invariants(m, got[0], got[1], got[2] if T else None, hs)
+    assert abs(i1["mass"] / i0["mass"] - 1) < 1e-14
+    assert abs(i1["energy"] / i0["energy"] - 1) < (1e-7 if T else 1e-6)
+    if T:
+        assert np.all(np.abs(i1["tracer_mass"] / i0["tracer_mass"] - 1) < 1e-13)

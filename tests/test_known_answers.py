@@ -5,7 +5,8 @@ import numpy as np
 
 import mpaso
 from mpaso.setup import fct_statics
-from mpaso.testcases import del2_mode, ocean_case, ocean_case_error, sw_case1, sw_case1_error
+from mpaso.testcases import (del2_mode, ocean_case, ocean_case_error, sw_case1, sw_case1_error, sw_case5, sw_case6,
+                             sw_invariants)
 from oracle import Oracle
 
 # ocean test cases (apps/ocean/tasks/testcase.cc): (dt, days) per icosahedral level
@@ -86,3 +87,39 @@ def test_ocean_case2_slotted_cylinder_stays_in_range():
     m, tr0, out, t = ocean_run(4, 2)
     assert out.max() <= 100.0 and out.min() > 50.0 * (1 - 2e-3)
     assert ocean_case_error(m, 2, out, t)[0] < 2.5e-3
+
+
+def sw_case_run(case, level=4, dt=600.0, n=144):
+    """One day of sw case 5 (with its two cone tracers, FCT) or 6 on the oracle."""
+    S = Oracle("restatement")
+    m = mpaso.Mesh.icosa(level)
+    if case == 6:
+        h, u = sw_case6(m)
+        hs, tr, T, st, opts = None, np.zeros((m.nCells, 1, 0)), 0, S.static(m), {}
+    else:
+        h, u, hs, tr = sw_case5(m)
+        T, st, opts = 2, S.static(m, fct_statics(m, 1), bottomDepth=hs), {"fct": True}
+    out = S.sw_run(m, st, S.config(1, T, **opts), dt, n, h, u, tr)
+    return m, (h, u, tr, hs), out
+
+
+def test_sw_case6_rossby_haurwitz_conserves_mass_and_energy():
+    """Case 6 for a day at level 4: mass to roundoff, total energy to 1e-6 (TRiSK
+    conserves energy in space; RK4 in time loses 6.5e-8 here)."""
+    m, (h, u, _, _), (hn, un, _) = sw_case_run(6)
+    i0, i1 = sw_invariants(m, h, u), sw_invariants(m, hn, un)
+    assert abs(i1["mass"] / i0["mass"] - 1) < 1e-14
+    assert abs(i1["energy"] / i0["energy"] - 1) < 1e-6
+
+
+def test_sw_case5_mountain_conserves_mass_tracers_and_bounds():
+    """Case 5 for a day at level 4 with its two cone tracers under FCT: mass and
+    tracer mass to roundoff, energy to 1e-7, tracers inside their initial range
+    up to 1e-6 (the limiter bounds against the full-dt provisional thickness, the
+    RK substeps use fractions of dt)."""
+    m, (h, u, tr, hs), (hn, un, trn) = sw_case_run(5)
+    i0, i1 = sw_invariants(m, h, u, tr, hs), sw_invariants(m, hn, un, trn, hs)
+    assert abs(i1["mass"] / i0["mass"] - 1) < 1e-14
+    assert np.all(np.abs(i1["tracer_mass"] / i0["tracer_mass"] - 1) < 1e-13)
+    assert abs(i1["energy"] / i0["energy"] - 1) < 1e-7
+    assert trn.min() > -1e-6 and trn.max() <= tr.max()
