@@ -349,6 +349,18 @@ def adjoint_arm(args):
     out = {}
     t_vjp = timed(lambda: out.update(g=st.vjp(gh_N, np.zeros_like(u0))))
     gh, gu = out["g"]
+    # the same gradient with the whole window stored (ckpt_every = 0): no recompute
+    st.set(G.FIELD_H, h0), st.set(G.FIELD_U, u0)
+    st.forward(dt, N, 0)
+    st.vjp(gh_N, np.zeros_like(u0))  # warm-up: captures the stored-mode graphs
+    st.set(G.FIELD_H, h0), st.set(G.FIELD_U, u0)
+    t_fwd_s = timed(lambda: st.forward(dt, N, 0))
+    t_vjp_s = timed(lambda: out.update(gs=st.vjp(gh_N, np.zeros_like(u0))))
+    stored = {"forward_ms": t_fwd_s, "vjp_ms": t_vjp_s, "vjp_over_plain_forward": t_vjp_s / t_plain,
+              "gradient_over_plain_forward": (t_fwd_s + t_vjp_s) / t_plain,
+              "max_rel_diff_vs_checkpointed": float(max(np.abs(a - b).max() / np.abs(b).max()
+                                                        for a, b in zip(out["gs"], (gh, gu)))),
+              "adjoint_device_bytes": int(st.adjoint_device_bytes())}
     rng = np.random.default_rng(7)
     errs = []
     for _ in range(args.adj_dirs):
@@ -372,7 +384,7 @@ def adjoint_arm(args):
             "vjp_over_plain_forward": t_vjp / t_plain,
             "fd_check": {"directions": args.adj_dirs, "max_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None},
-            "peak_device_bytes": int(mem), "tracers": tracers}
+            "peak_device_bytes": int(mem), "stored_window": stored, "tracers": tracers}
 
 
 def adjoint_tracer_leg(args, mesh, N, K, dt):
@@ -424,6 +436,16 @@ def adjoint_tracer_leg(args, mesh, N, K, dt):
     out = {}
     t_vjp = timed(lambda: out.update(g=st.vjp_tracers(zh, zu, gtr_N)))
     gh, gu, gt = out["g"]
+    put(h0, u0, tr0)
+    st.forward(dt, N, 0)
+    st.vjp_tracers(zh, zu, gtr_N)
+    put(h0, u0, tr0)
+    t_fwd_s = timed(lambda: st.forward(dt, N, 0))
+    t_vjp_s = timed(lambda: out.update(gs=st.vjp_tracers(zh, zu, gtr_N)))
+    stored = {"forward_ms": t_fwd_s, "vjp_ms": t_vjp_s, "vjp_over_plain_forward": t_vjp_s / t_plain,
+              "gradient_over_plain_forward": (t_fwd_s + t_vjp_s) / t_plain,
+              "bitwise_equal_to_checkpointed": bool(all(np.array_equal(a, b) for a, b in zip(out["gs"], (gh, gu, gt)))),
+              "adjoint_device_bytes": int(st.adjoint_device_bytes())}
     rng = np.random.default_rng(8)
     errs = []
     for _ in range(min(args.adj_dirs, 4)):
@@ -436,7 +458,7 @@ def adjoint_tracer_leg(args, mesh, N, K, dt):
         errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
     return {"workload": "same window, 1 tracer (FCT + del2 kappa=1e4), loss on the final tracer",
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
-            "vjp_over_plain_forward": t_vjp / t_plain,
+            "vjp_over_plain_forward": t_vjp / t_plain, "stored_window": stored,
             "fd_check": {"directions": len(errs), "max_rel_err": max(errs) if errs else None},
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
 

@@ -291,7 +291,9 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
  *
  * mpaso_rk4_forward: advances the state nsteps steps of size dt like
  * mpaso_rk4_step, keeping a checkpoint of (h, u, tracers) every ckpt_every
- * steps.
+ * steps.  ckpt_every = 0 stores the whole window instead (every stage state
+ * and the intermediates the reverse sweep reads, 4 nsteps + 1 tape slots),
+ * so the vjp recomputes nothing: HBM for time, where the window fits.
  * mpaso_rk4_vjp: given the cotangents gh (nCells x nlev) and gu (nEdges x
  * nlev) of the state after the forward run, writes dJ/dh0 and dJ/du0 of the
  * state before it into gh0 / gu0 (reference ordering; host or device

@@ -81,14 +81,25 @@ struct AdjBuffers {
   // the whole reverse sweep, captured once per (N, k, dt, tracers) and replayed
   cudaGraphExec_t rev = nullptr;
   int rev_N = 0, rev_k = 0, rev_tr = 0;
+  bool rev_stored = false;
   double rev_dt = 0.0;
   int tr = 0;  // the sweep being run reverses the tracers too
+  // ckpt_every = 0: the forward tapes the whole window (one segment), the
+  // reverse sweep recomputes nothing; the taping forward is a captured graph
+  bool stored = false, stored_tr = false;
+  cudaGraphExec_t fwd = nullptr;
+  int fwd_N = 0;
+  double fwd_dt = 0.0;
 };
 
 void drop_adjoint_graph(SwState &s) {
   if (s.adj && s.adj->rev) {
     cudaGraphExecDestroy(s.adj->rev);
     s.adj->rev = nullptr;
+  }
+  if (s.adj && s.adj->fwd) {
+    cudaGraphExecDestroy(s.adj->fwd);
+    s.adj->fwd = nullptr;
   }
 }
 
@@ -712,12 +723,62 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
   launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
 }
 
+void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t st);
+
+// Captures (once per window length and dt) and replays the taping forward of
+// the store-the-window mode, then leaves the final state in the state's buffers.
+void forward_stored(SwState &s, double dt, int N) {
+  AdjBuffers &A = *s.adj;
+  const DMesh &m = s.mesh->ctx.d;
+  const size_t eu = (size_t)m.nE * s.L, ch = (size_t)m.nC * s.L, ct = ch * s.T;
+  const bool with_tr = s.T > 0;
+  if (A.fwd && (A.fwd_N != N || A.fwd_dt != dt)) {
+    cudaGraphExecDestroy(A.fwd);
+    A.fwd = nullptr;
+  }
+  if (!A.fwd) {
+    cudaGraph_t g;
+    MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_u, s.U[0], eu * 8, cudaMemcpyDeviceToDevice, s.stream));
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_h, s.H[0], ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      if (with_tr) MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, s.TR0, ct * 8, cudaMemcpyDeviceToDevice, s.stream));
+      tape_segment(s, A, N, with_tr, s.stream);
+      MPASO_CUDA(cudaMemcpyAsync(s.U[0], A.tp_u + 4 * (size_t)N * eu, eu * 8, cudaMemcpyDeviceToDevice, s.stream));
+      MPASO_CUDA(cudaMemcpyAsync(s.H[0], A.tp_h + 4 * (size_t)N * ch, ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      if (with_tr)
+        MPASO_CUDA(cudaMemcpyAsync(s.TR0, A.tp_tr + 4 * (size_t)N * ct, ct * 8, cudaMemcpyDeviceToDevice, s.stream));
+    } catch (...) {
+      cudaStreamEndCapture(s.stream, &g);
+      cudaGetLastError();
+      throw;
+    }
+    MPASO_CUDA(cudaStreamEndCapture(s.stream, &g));
+    const cudaError_t e = cudaGraphInstantiate(&A.fwd, g, 0);
+    cudaGraphDestroy(g);
+    MPASO_CUDA(e);
+    A.fwd_N = N, A.fwd_dt = dt;
+  }
+  MPASO_CUDA(cudaGraphLaunch(A.fwd, s.stream));
+  s.diag_valid = false;  // the taping stages wrote the state's diagnostic scratch
+  A.stored_tr = with_tr;
+}
+
 void forward(SwState &s, double dt, int N, int k) {
   require(s.p.app == MPASO_APP_SW, MPASO_ERR_ARG, "the adjoint covers the sw app");
   require(!s.p.pin_u, MPASO_ERR_ARG, "the adjoint does not support a pinned wind (test case 1)");
-  require(N >= 1 && k >= 1, MPASO_ERR_ARG, "nsteps and ckpt_every must be >= 1");
+  require(N >= 1 && k >= 0, MPASO_ERR_ARG, "nsteps must be >= 1 and ckpt_every >= 0");
+  const bool stored = k == 0;
+  if (stored) k = N;
   ensure_buffers(s, N, k);
   AdjBuffers &A = *s.adj;
+  A.stored = stored;
+  if (stored) {
+    A.N = N, A.k = N, A.dt = dt, A.nck = 1;
+    forward_stored(s, dt, N);
+    A.have_forward = true;
+    return;
+  }
   const DMesh &m = s.mesh->ctx.d;
   const size_t eu = (size_t)m.nE * s.L * 8, ch = (size_t)m.nC * s.L * 8;
   A.N = N, A.k = k, A.dt = dt, A.nck = (N + k - 1) / k;
@@ -740,49 +801,61 @@ void forward(SwState &s, double dt, int N, int k) {
   A.have_forward = true;
 }
 
+// Taping run of n steps from tape slot 0 (state there already): slot 4t + rk
+// receives the input of stage rk of step t, plus the stage's pv and kite-summed
+// thickness, and with tracers the stage's fluxes, limiter factors, upwind sums
+// and 1/hProv.  with_tr: the tracer-carrying stage kernels (else (h, u) only).
+void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
+  const int64_t cT = ch * s.T, eT = eu * s.T;
+  const int64_t vv = (int64_t)m.nV * s.L;
+  sw_diag_ptrs(s, A.tp_u, A.tp_h, A.tp_pv, A.tp_hs, st);
+  for (int t = 0; t < n; ++t) {
+    double *yu = A.tp_u + (size_t)4 * t * eu, *yh = A.tp_h + (size_t)4 * t * ch;
+    for (int rk = 0; rk < 4; ++rk) {
+      double *iu = yu + (size_t)rk * eu, *ih = yh + (size_t)rk * ch;
+      double *ou = yu + (size_t)(rk + 1) * eu, *oh = yh + (size_t)(rk + 1) * ch;
+      const size_t next = (size_t)(4 * t + rk + 1) * vv;  // tape slot of the stage's output
+      if (!with_tr) {
+        sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc, A.hacc,
+                      rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next, A.tp_hs + next, st);
+        continue;
+      }
+      // with tracers: the state's own stage kernels, every pointer on the tape
+      const int j = 4 * t + rk;
+      double *ytr = A.tp_tr + (size_t)4 * t * cT;
+      Stage S = sw_make_stage(s, rk, A.dt);
+      S.u_in = iu, S.h_in = ih, S.tr_in = ytr + (size_t)rk * cT;
+      S.u_prev = yu, S.h_prev = yh, S.tr_prev = ytr;
+      S.u_out = rk < 3 ? ou : nullptr, S.h_out = rk < 3 ? oh : nullptr;
+      S.tr_out = rk < 3 ? ytr + (size_t)(rk + 1) * cT : nullptr;
+      S.u_acc = A.uacc, S.h_acc = A.hacc, S.trh_acc = A.trhacc;
+      S.u_new = rk == 3 ? ou : nullptr, S.h_new = rk == 3 ? oh : nullptr;
+      S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
+      S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
+      S.tLO = A.tp_tLO + (size_t)j * cT, S.tape_hpi = A.tp_hpi + (size_t)j * ch;
+      S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next;
+      sw_launch_stage(s, S, st);
+    }
+  }
+}
+
 void reverse_body(SwState &s) {
   AdjBuffers &A = *s.adj;
   const DMesh &m = s.mesh->ctx.d;
   const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
-  const int64_t cT = ch * s.T, eT = eu * s.T;
+  const int64_t cT = ch * s.T;
   const cudaStream_t st = s.stream;
   for (int seg = A.nck - 1; seg >= 0; --seg) {
     const int s0 = seg * A.k, n = std::min(A.k, A.N - s0);
-    // taping recompute of the segment: slot 4t + rk holds the input of stage rk of step s0 + t
-    MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
-    MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
-    if (A.tr)
-      MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, st));
-    const int64_t vv = (int64_t)m.nV * s.L;
-    sw_diag_ptrs(s, A.tp_u, A.tp_h, A.tp_pv, A.tp_hs, st);
-    for (int t = 0; t < n; ++t) {
-      double *yu = A.tp_u + (size_t)4 * t * eu, *yh = A.tp_h + (size_t)4 * t * ch;
-      for (int rk = 0; rk < 4; ++rk) {
-        double *iu = yu + (size_t)rk * eu, *ih = yh + (size_t)rk * ch;
-        double *ou = yu + (size_t)(rk + 1) * eu, *oh = yh + (size_t)(rk + 1) * ch;
-        const size_t next = (size_t)(4 * t + rk + 1) * vv;  // tape slot of the stage's output
-        if (!A.tr) {
-          sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc,
-                        A.hacc, rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next,
-                        A.tp_hs + next, st);
-          continue;
-        }
-        // with tracers: the state's own stage kernels, every pointer on the tape
-        const int j = 4 * t + rk;
-        double *ytr = A.tp_tr + (size_t)4 * t * cT;
-        Stage S = sw_make_stage(s, rk, A.dt);
-        S.u_in = iu, S.h_in = ih, S.tr_in = ytr + (size_t)rk * cT;
-        S.u_prev = yu, S.h_prev = yh, S.tr_prev = ytr;
-        S.u_out = rk < 3 ? ou : nullptr, S.h_out = rk < 3 ? oh : nullptr;
-        S.tr_out = rk < 3 ? ytr + (size_t)(rk + 1) * cT : nullptr;
-        S.u_acc = A.uacc, S.h_acc = A.hacc, S.trh_acc = A.trhacc;
-        S.u_new = rk == 3 ? ou : nullptr, S.h_new = rk == 3 ? oh : nullptr;
-        S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
-        S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
-        S.tLO = A.tp_tLO + (size_t)j * cT, S.tape_hpi = A.tp_hpi + (size_t)j * ch;
-        S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next;
-        sw_launch_stage(s, S, st);
-      }
+    if (!A.stored) {
+      // taping recompute of the segment from its checkpoint
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
+      if (A.tr)
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, st));
+      tape_segment(s, A, n, A.tr != 0, st);
     }
     if (seg == A.nck - 1) {
       // cotangents of the final state (tape slot 4n): tracers to q = h tr, then
@@ -811,7 +884,10 @@ void reverse_body(SwState &s) {
 // once as a graph for the current (N, k, dt) and buffers, then replayed.
 void reverse(SwState &s) {
   AdjBuffers &A = *s.adj;
-  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt || A.rev_tr != A.tr)) drop_adjoint_graph(s);
+  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt || A.rev_tr != A.tr || A.rev_stored != A.stored)) {
+    cudaGraphExecDestroy(A.rev);
+    A.rev = nullptr;
+  }
   if (!A.rev) {
     cudaGraph_t g;
     MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
@@ -826,7 +902,7 @@ void reverse(SwState &s) {
     const cudaError_t e = cudaGraphInstantiate(&A.rev, g, 0);
     cudaGraphDestroy(g);
     MPASO_CUDA(e);
-    A.rev_N = A.N, A.rev_k = A.k, A.rev_dt = A.dt, A.rev_tr = A.tr;
+    A.rev_N = A.N, A.rev_k = A.k, A.rev_dt = A.dt, A.rev_tr = A.tr, A.rev_stored = A.stored;
   }
   MPASO_CUDA(cudaGraphLaunch(A.rev, s.stream));
   s.diag_valid = false;
@@ -900,6 +976,7 @@ int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, con
     require(S.adj && S.adj->have_forward, MPASO_ERR_ARG,
             "mpaso_rk4_vjp_tracers needs a preceding mpaso_rk4_forward");
     require(!S.p.fct || S.mesh->ctx.has_fct, MPASO_ERR_ARG, "FCT statics missing from the mesh");
+    require(!S.adj->stored || S.adj->stored_tr, MPASO_ERR_ARG, "the stored window holds no tracers");
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     const int64_t LT = (int64_t)S.L * S.T;
     to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);

@@ -319,7 +319,8 @@ class State:
 
     # ---- differentiation (sw app: h and u) ----
     def forward(self, dt, nsteps, ckpt_every):
-        """Advances nsteps from the current (h, u), keeping a checkpoint every ckpt_every steps."""
+        """Advances nsteps from the current (h, u), keeping a checkpoint every ckpt_every steps
+        (0: the whole window is stored and the vjp recomputes nothing)."""
         check(lib().mpaso_rk4_forward(self._h, ctypes.c_double(dt), int(nsteps), int(ckpt_every)))
 
     def vjp(self, gh, gu, out=None):

@@ -54,7 +54,7 @@ def test_checkpoint_interval_does_not_change_gradient():
     rng = np.random.default_rng(2)
     wh, wu = rng.standard_normal(h.shape), rng.standard_normal(u.shape)
     grads = []
-    for k in (1, 3, 7):
+    for k in (1, 3, 7, 0):  # 0: the window stored, no recompute
         st.set(G.FIELD_H, h)
         st.set(G.FIELD_U, u)
         st.forward(450.0, 7, k)

@@ -121,3 +121,27 @@ def test_tracer_adjoint_checkpoint_interval_and_hu_consistency():
     assert np.all(gt == 0.0)
     gh2, gu2 = st.vjp(w[0], w[1])
     assert np.array_equal(gh, gh2) and np.array_equal(gu, gu2)
+
+
+def test_stored_window_gives_the_checkpointed_gradient():
+    """ckpt_every = 0 tapes the whole window during the forward: same final state
+    and, for the tracer vjp (same kernels both ways), the same gradient bit for
+    bit as checkpointing; the (h, u) vjp (tracer-free recompute kernels when
+    checkpointing) agrees to rounding."""
+    import mpaso.gpu as G
+    L, T, dt, n = 1, 2, 300.0, 5
+    mesh, f, st, (h, u, tr) = make(L, T, True, True, level=2)
+    rng = np.random.default_rng(9)
+    w = (rng.standard_normal(h.shape), rng.standard_normal(u.shape), rng.standard_normal(tr.shape))
+    out = {}
+    for k in (2, 0):
+        set_state(st, h, u, tr)
+        st.forward(dt, n, k)
+        fin = (st.get(G.FIELD_H), st.get(G.FIELD_U), st.get(G.FIELD_TRACERS))
+        out[k] = (fin, st.vjp_tracers(*w), st.vjp(w[0], w[1]))
+    for a, b in zip(out[0][0], out[2][0]):
+        assert np.array_equal(a, b)
+    for a, b in zip(out[0][1], out[2][1]):
+        assert np.array_equal(a, b)
+    for a, b in zip(out[0][2], out[2][2]):
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
