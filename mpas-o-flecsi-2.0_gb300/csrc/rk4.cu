@@ -315,6 +315,10 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
 SwState::~SwState() {
   if (graph) cudaGraphExecDestroy(graph);
   if (xg) cudaGraphExecDestroy(xg);
+  for (auto &x : x_side)
+    if (x) cudaStreamDestroy(x);
+  for (auto &e : x_ev)
+    if (e) cudaEventDestroy(e);
   if (out_stream) cudaStreamSynchronize(out_stream);
   for (int b = 0; b < 2; ++b) {
     if (out_buf[b]) cudaFree(out_buf[b]);
@@ -493,6 +497,7 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
     launch_k2<T, 0, 0>(s, S, u2, s.tune_tpb[1], st);
   }
   if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
+  if (s.k2_mark) MPASO_CUDA(cudaEventRecord(s.k2_mark, st));
   if (OC1 && s.tune_occ[2])
     launch_k3<T, OC1>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
   else
@@ -982,38 +987,92 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
       MPASO_CUDA(cudaGraphExecDestroy(S.xg));
       S.xg = nullptr;
     }
+    if (locked && !S.x_side[0]) {
+      for (auto &x : S.x_side) MPASO_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      for (auto &e : S.x_ev) MPASO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
     if (locked) MPASO_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     // one copy per field each way (copy engines; page-locked buffers go at link speed),
     // the permutations on the device, one synchronisation.  (Letting the permutation
     // kernels read and write mapped host memory directly was slower: their accesses
     // are scattered.)
     try {
-    MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
-    MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (tr) MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, st));
-    k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
-    k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
-    if (tr) k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
-    if (locked) {  // inside the capture: the steps' kernels themselves
-      if (S.p.app == MPASO_APP_SW) {
+    if (!locked) {
+      MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
+      MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, st));
+      if (tr) MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, st));
+      k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+      k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+      if (tr) k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+      S.diag_valid = false;
+      S.prep_dt = 0.0;
+      step_graph(S, dt, nsteps);
+      k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+      k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
+      if (tr) k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
+      MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, st));
+      MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, st));
+      if (tr) MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    } else {
+      // Captured as a DAG over the state stream and two side streams: each field's
+      // permutation starts when its own copy lands; the diagnostics wait for h and
+      // u only, the steps for the tracers too; h and u go back out as soon as the
+      // last stage's tendency kernel has written them, under that stage's tracer
+      // kernel, and the tracers after it.
+      const cudaStream_t su = S.x_side[0], sx = S.x_side[1];
+      cudaEvent_t *E = S.x_ev;
+      MPASO_CUDA(cudaEventRecord(E[0], st));
+      MPASO_CUDA(cudaStreamWaitEvent(su, E[0], 0));
+      MPASO_CUDA(cudaStreamWaitEvent(sx, E[0], 0));
+      MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
+      k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+      MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, su));
+      k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
+      MPASO_CUDA(cudaEventRecord(E[1], su));
+      if (tr) {
+        MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, sx));
+        k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
+      }
+      MPASO_CUDA(cudaEventRecord(E[2], sx));
+      MPASO_CUDA(cudaStreamWaitEvent(st, E[1], 0));
+      const bool sw = S.p.app == MPASO_APP_SW;
+      if (sw) {
         S.diag_valid = false;
         ensure_diag(S, st);
       } else {
         ocean_recompute(S, dt, st);
       }
-      run_steps(S, dt, nsteps, st);
-    } else {
-      S.diag_valid = false;
-      S.prep_dt = 0.0;
-      step_graph(S, dt, nsteps);
+      MPASO_CUDA(cudaStreamWaitEvent(st, E[2], 0));
+      if (sw && nsteps > 0) {
+        for (int n = 0; n < nsteps; ++n)
+          for (int rk = 0; rk < 4; ++rk) {
+            if (n == nsteps - 1 && rk == 3) S.k2_mark = E[3];
+            launch_stage(S, make_stage(S, rk, dt), st);
+            S.k2_mark = nullptr;
+          }
+      } else {
+        run_steps(S, dt, nsteps, st);
+        MPASO_CUDA(cudaEventRecord(E[3], st));
+      }
+      MPASO_CUDA(cudaEventRecord(E[5], st));
+      MPASO_CUDA(cudaStreamWaitEvent(su, E[3], 0));
+      k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
+      MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, su));
+      MPASO_CUDA(cudaEventRecord(E[4], su));
+      MPASO_CUDA(cudaStreamWaitEvent(sx, E[3], 0));
+      k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, sx);
+      MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, sx));
+      if (tr) {
+        MPASO_CUDA(cudaStreamWaitEvent(sx, E[5], 0));
+        k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
+        MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, sx));
+      }
+      MPASO_CUDA(cudaEventRecord(E[6], sx));
+      MPASO_CUDA(cudaStreamWaitEvent(st, E[4], 0));  // join the side streams before the capture ends
+      MPASO_CUDA(cudaStreamWaitEvent(st, E[6], 0));
     }
-    k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
-    k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, st);
-    if (tr) k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), st);
-    MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, st));
-    MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (tr) MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
     } catch (...) {
+      S.k2_mark = nullptr;
       if (locked) {
         cudaGraph_t g;
         cudaStreamEndCapture(st, &g);

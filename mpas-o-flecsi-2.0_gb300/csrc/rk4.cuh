@@ -130,9 +130,16 @@ struct SwState {
   // device staging of mpaso_rk4_step_host (reference-ordered h, u, tracers)
   double *io_stage = nullptr;
   size_t io_bytes = 0;
-  // mpaso_rk4_step_host with page-locked buffers: the captured exchange graph
+  // mpaso_rk4_step_host with page-locked buffers: the captured exchange graph,
+  // a DAG over the state stream and two side streams (one per field) so each
+  // field's copy and permutation overlap the others'
   cudaGraphExec_t xg = nullptr;
   XKey xkey{};
+  cudaStream_t x_side[2] = {nullptr, nullptr};
+  cudaEvent_t x_ev[7] = {};
+  // when set, recorded on the stage stream right after the tendency kernel of
+  // each stage launched (h and u of that stage's output are final there)
+  cudaEvent_t k2_mark = nullptr;
   // history output (mpaso_state_snapshot): side stream, two staging buffers
   // used in turn, events ordering them against the stepping stream
   cudaStream_t out_stream = nullptr;

@@ -145,3 +145,23 @@ def test_stored_window_gives_the_checkpointed_gradient():
         assert np.array_equal(a, b)
     for a, b in zip(out[0][2], out[2][2]):
         assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+
+
+def test_autograd_function_with_tracers():
+    """RK4Tracers through torch.autograd gives the raw vjp_tracers gradient."""
+    torch = pytest.importorskip("torch")
+    from mpaso.autograd import RK4Tracers
+    L, T, dt, n = 1, 1, 300.0, 3
+    mesh, f, st, (h, u, tr) = make(L, T, True, True, level=3)
+    target = torch.from_numpy(tr * 0.9).cuda()
+    h0 = torch.from_numpy(h).cuda().requires_grad_(True)
+    u0 = torch.from_numpy(u).cuda().requires_grad_(True)
+    t0 = torch.from_numpy(tr).cuda().requires_grad_(True)
+    hN, uN, tN = RK4Tracers.apply(st, h0, u0, t0, dt, n, 0)
+    loss = 0.5 * ((tN - target) ** 2).sum()
+    loss.backward()
+    set_state(st, h, u, tr)
+    st.forward(dt, n, 0)
+    g = st.vjp_tracers(np.zeros_like(h), np.zeros_like(u), (tN - target).detach().cpu().numpy())
+    for got, want in zip((h0.grad, u0.grad, t0.grad), g):
+        assert np.allclose(got.cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())
