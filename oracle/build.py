@@ -88,6 +88,44 @@ def build_ref(force=False):
         return out
 
 
+def build_flecsi_wrappers(force=False):
+    """oracle/_ref/libref_gb300_L1_T1.so: the reference's own driver logic
+    (ref_driver.cc) and FCT setup (init_functions.cc) with the FleCSI wrapper
+    library's task bodies (mpas-o-flecsi-2.0_gb300/flecsi/) in place of the
+    reference's apps/sw/tasks/solve.cc and apps/ocean/tasks/solve.cc, linked
+    against libmpaso: it links only if every task the driver calls is defined
+    with the reference's declared signature.  None without a checkout."""
+    if not ref_available():
+        return None
+    pkg = os.path.join(os.path.dirname(HERE), "mpas-o-flecsi-2.0_gb300")
+    wrap = os.path.join(pkg, "flecsi")
+    lib_dir = os.path.join(pkg, "lib")
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    shim = os.path.join(HERE, "shim")
+    srcs = [os.path.join(REF, "apps/ocean/tasks/init_functions.cc"), os.path.join(HERE, "ref_driver.cc"),
+            os.path.join(HERE, "flecsi_probe.cc"), os.path.join(wrap, "sw_tasks.cc"),
+            os.path.join(wrap, "ocean_tasks.cc")]
+    deps = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs] + srcs + [
+        os.path.join(wrap, "mpaso_flecsi.hh"), os.path.join(HERE, "build.py"), os.path.join(HERE, "sw_extra.c"),
+        os.path.join(os.path.dirname(HERE), "include", "mpaso.h")]
+    out = os.path.join(out_dir, "libref_gb300_L1_T1.so")
+    if not (force or _stale(out, deps)):
+        return out
+    defs = ["-DMPASO_REF_NVL=1", "-DMPASO_REF_NTR=1", f"-DMPASO_REF_GRAVITY={GRAVITY}"]
+    inc = [f"-I{shim}", f"-I{REF}", f"-I{HERE}", f"-I{wrap}", f"-I{os.path.join(os.path.dirname(HERE), 'include')}"]
+    objs = []
+    for src in srcs:
+        obj = os.path.join(out_dir, "gb300_" + os.path.basename(src) + ".o")
+        _run(["g++", "-std=c++17", *CFLAGS, *defs, *inc, "-w", "-c", src, "-o", obj])
+        objs.append(obj)
+    obj = os.path.join(out_dir, "gb300_sw_extra.o")
+    _run(["gcc", "-std=c11", *CFLAGS, f"-I{HERE}", "-c", os.path.join(HERE, "sw_extra.c"), "-o", obj])
+    objs.append(obj)
+    _run(["g++", "-shared", "-o", out, *objs, f"-L{lib_dir}", "-lmpaso", f"-Wl,-rpath,{lib_dir}", "-lm"])
+    return out
+
+
 CSTEP_LEVELS = 2  # levels of the complex-step build of the sw tasks
 
 
