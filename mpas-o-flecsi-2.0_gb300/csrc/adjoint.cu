@@ -58,6 +58,7 @@ struct AdjBuffers {
   double *tp_u = nullptr, *tp_h = nullptr;  // stage-state tape [4k + 1][...]
   double *uacc = nullptr, *hacc = nullptr;
   double *tp_pv = nullptr, *tp_hs = nullptr;  // pv, kite-summed h of every tape slot [4k + 1][nV L]
+  double *tp_s1 = nullptr;  // the forward's TRiSK sum sum_j W_j F_j / 4 of every stage [4k][nE L]
   double *pve = nullptr;
   double2 *FP = nullptr;  // {F, P} per edge, gathered together by B1
   double *lam_u = nullptr, *lam_h = nullptr, *acc_u = nullptr, *acc_h = nullptr;
@@ -119,6 +120,7 @@ constexpr int TPB = 256;
 struct AdjArgs {
   const double *u, *h;                        // stage state
   const double *pv, *hs;                      // taped pv, kite-summed h of the stage state
+  const double *s1;                           // taped TRiSK sum of the stage (sum W F / 4)
   double *pve;                                // edge pv of the stage state
   double2 *FP;                                // {F = u he, P = lk_u pve} per edge
   const double *un, *hn, *pvn;                // state of the next stage to reverse (prep)
@@ -180,17 +182,17 @@ __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= (int64_t)m.nE * L) return;
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
-  double s1 = 0.0, t1 = 0.0, t2 = 0.0;
+  // S1 = sum_j W_j F_j comes from the forward's tape (4 x its W/8 . 2F sum, exact)
+  const double s1 = 4.0 * a.s1[i];
+  double t1 = 0.0, t2 = 0.0;
   const int ne = NW > 0 ? NW : m.maxEoE;
 #pragma unroll
   for (int j = 0; j < ne; ++j) {
     const int64_t s = (int64_t)j * m.nE + e;
     const int64_t io = (int64_t)m.eoe[s] * L + k;
     const double wt = m.woeT[s];
-    const double2 fp = a.FP[io];
-    s1 = fma(m.woe[s], fp.x, s1);
     t1 = fma(wt, a.lk_u[io], t1);
-    t2 = fma(wt, fp.y, t2);
+    t2 = fma(wt, a.FP[io].y, t2);
   }
   const int2 c = m.coe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
@@ -639,7 +641,7 @@ void ensure_buffers(SwState &s, int N, int k) {
   std::vector<std::pair<double **, int64_t>> bufs = {
       {&A->ck_u, nck * eu}, {&A->ck_h, nck * ch}, {&A->tp_u, (4LL * k + 1) * eu},
       {&A->tp_h, (4LL * k + 1) * ch}, {&A->uacc, eu}, {&A->hacc, ch}, {&A->tp_pv, (4LL * k + 1) * vv},
-      {&A->tp_hs, (4LL * k + 1) * vv},
+      {&A->tp_hs, (4LL * k + 1) * vv}, {&A->tp_s1, 4LL * k * eu},
       {(double **)&A->FP, 2 * eu}, {&A->pve, eu}, {&A->lam_u, eu}, {&A->lam_h, ch}, {&A->acc_u, eu},
       {&A->acc_h, ch}, {&A->lk_u, eu}, {&A->lk_h, ch}, {&A->mu_u, eu}, {&A->mu_h, ch}, {&A->lhe, eu},
       {&A->lpve, eu}, {&A->lke, ch}, {&A->ldiv, ch}, {&A->lcirc, vv}, {&A->lhs, vv}};
@@ -681,6 +683,7 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
   AdjArgs a{};
   a.u = A.tp_u + (size_t)j * nE, a.h = A.tp_h + (size_t)j * nC;
   a.pv = A.tp_pv + (size_t)j * nV, a.hs = A.tp_hs + (size_t)j * nV;
+  a.s1 = A.tp_s1 + (size_t)j * nE;
   a.FP = A.FP, a.pve = A.pve;
   a.lk_u = A.lk_u, a.lk_h = A.lk_h, a.mu_u = A.mu_u, a.mu_h = A.mu_h;
   a.lhe = A.lhe, a.lpve = A.lpve, a.lke = A.lke, a.ldiv = A.ldiv, a.lcirc = A.lcirc, a.lhs = A.lhs;
@@ -819,7 +822,8 @@ void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t s
       const size_t next = (size_t)(4 * t + rk + 1) * vv;  // tape slot of the stage's output
       if (!with_tr) {
         sw_stage_ptrs(s, rk, A.dt, iu, ih, yu, yh, rk < 3 ? ou : nullptr, rk < 3 ? oh : nullptr, A.uacc, A.hacc,
-                      rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next, A.tp_hs + next, st);
+                      rk == 3 ? ou : nullptr, rk == 3 ? oh : nullptr, A.tp_pv + next, A.tp_hs + next,
+                      A.tp_s1 + (size_t)(4 * t + rk) * eu, st);
         continue;
       }
       // with tracers: the state's own stage kernels, every pointer on the tape
@@ -835,7 +839,7 @@ void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t s
       S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
       S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
       S.tLO = A.tp_tLO + (size_t)j * cT, S.tape_hpi = A.tp_hpi + (size_t)j * ch;
-      S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next;
+      S.tape_pv = A.tp_pv + next, S.tape_hs = A.tp_hs + next, S.tape_s1 = A.tp_s1 + (size_t)j * eu;
       sw_launch_stage(s, S, st);
     }
   }

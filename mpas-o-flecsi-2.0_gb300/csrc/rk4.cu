@@ -82,6 +82,7 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
       s2 = fma(w, fg.y, s2);
     }
     const double q = fma(S.pve[i], s1, s2);
+    if (S.tape_s1) S.tape_s1[i] = s1;
     const int2 c = m.coe[e];
     const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
     // - (ke2 - ke1 + g (h2 + b2 - h1 - b1)) / dc + nu (div2 - div1) / dc, with the
@@ -570,12 +571,12 @@ void sw_create(SwState &s) {
 void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
                    const double *u_prev, const double *h_prev, double *u_out, double *h_out,
                    double *u_acc, double *h_acc, double *u_new, double *h_new, double *tape_pv,
-                   double *tape_hs, cudaStream_t st) {
+                   double *tape_hs, double *tape_s1, cudaStream_t st) {
   Stage S = make_stage(s, rk, dt);
   S.u_in = u_in, S.h_in = h_in, S.u_prev = u_prev, S.h_prev = h_prev;
   S.u_out = u_out, S.h_out = h_out, S.u_acc = u_acc, S.h_acc = h_acc, S.u_new = u_new, S.h_new = h_new;
   S.fct = 0, S.hmix = 0;
-  S.tape_pv = tape_pv, S.tape_hs = tape_hs;
+  S.tape_pv = tape_pv, S.tape_hs = tape_hs, S.tape_s1 = tape_s1;
   launch_stage_T<0>(s, S, st);
 }
 

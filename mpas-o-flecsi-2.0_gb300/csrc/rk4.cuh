@@ -95,6 +95,7 @@ struct Stage {
   const double *hE, *hpi;                   // ocean: layerThicknessEdge, 1/hProv
   double *tape_pv, *tape_hs;                // adjoint taping: pv and kite-summed h of the next state
   double *tape_hpi;                         // adjoint taping: 1/hProv of the stage (FCT)
+  double *tape_s1;                          // adjoint taping: sum_j W_j F2_j / 8 of each edge
   double *hpw;                              // sw four-launch schedule: 1/hProv from K2 to the limiter
 };
 
@@ -180,7 +181,7 @@ void free_adjoint(SwState &s);
 void sw_stage_ptrs(SwState &s, int rk, double dt, const double *u_in, const double *h_in,
                    const double *u_prev, const double *h_prev, double *u_out, double *h_out,
                    double *u_acc, double *h_acc, double *u_new, double *h_new, double *tape_pv,
-                   double *tape_hs, cudaStream_t st);
+                   double *tape_hs, double *tape_s1, cudaStream_t st);
 void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv, double *tape_hs,
                   cudaStream_t st);
 void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
