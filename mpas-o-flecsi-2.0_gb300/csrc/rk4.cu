@@ -386,7 +386,7 @@ Stage make_stage(SwState &s, int rk, double dt) {
   const double rk_sub[4] = {dt / 2, dt / 2, dt, 0};
   Stage S{};
   S.stage = rk, S.w_sub = rk_sub[rk], S.w_acc = rk_w[rk], S.dt = dt, S.g = s.p.gravity, S.nu = s.p.nu;
-  S.fct = s.p.fct, S.hmix = s.p.hmix, S.visc = s.p.nu != 0.0, S.pin_u = s.p.pin_u;
+  S.fct = s.p.fct, S.hmix = s.p.hmix, S.visc = s.p.nu != 0.0, S.pin_u = s.p.pin_u, S.centred = !s.p.fct;
   // buffer rotation: prev = 0, acc = 2, stage inputs 0 -> 1 -> 3 -> 1, new -> 0
   static const int uin[4] = {0, 1, 3, 1}, uout[4] = {1, 3, 1, -1};
   S.u_in = s.U[uin[rk]], S.h_in = s.H[uin[rk]];

@@ -81,6 +81,7 @@ struct Stage {
   double w_sub, w_acc;  // substep and accumulation weights (apps/sw/run.cc:23-24)
   double dt, g, nu;
   int fct, hmix, visc, pin_u;
+  int centred;          // without FCT: the sw app's centred tracer flux (1) or no advection (0, ocean)
   const double *u_in, *h_in, *tr_in;        // stage input
   const double *u_prev, *h_prev, *tr_prev;  // step start
   double *u_out, *h_out, *tr_out;           // next stage input (stages 0..2)
@@ -236,10 +237,14 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
       S.LO[i * T + t] = lo;
       S.A[i * T + t] = ho - lo;
     }
-  } else {
+  } else if (S.centred) {
     // centred flux of compute_scalar_tend (apps/sw/tasks/solve.cc:255-269)
 #pragma unroll
     for (int t = 0; t < T; ++t) S.LO[i * T + t] = (0.5 * dvF) * (t1[t] + t2[t]);
+  } else {
+    // the ocean app advects tracers only through FCT (apps/ocean/run.cc:20-38)
+#pragma unroll
+    for (int t = 0; t < T; ++t) S.LO[i * T + t] = 0.0;
   }
   if (S.hmix) {
     const double hk = hx * kd[e];

@@ -111,13 +111,15 @@ def sw_state(mesh, seed, nlev=1, ntr=1, h0=None, h_amp=None, u_peak=None, degree
     return h, u, tr
 
 
-def ocean_state(mesh, seed, nlev=60, ntr=3, layer_thickness=None, u_peak=0.3, degree=8):
+def ocean_state(mesh, seed, nlev=60, ntr=3, layer_thickness=None, u_peak=0.3, degree=8, clip=True):
     """Multi-layer ocean tracer state for the FCT/del2 tracer app.
 
     Layer thickness: uniform per level (default 100 m); velocity per level from
     a seeded streamfunction (peak `u_peak` m/s, decaying with depth);
     tracers: temperature 0-30 C decreasing linearly with depth, salinity
     34-36 psu, passive tracer 0-1, each with seeded smooth noise.
+    Temperature is clipped to [0, 30] (clip=True), which leaves plateaus at
+    exactly 0 and 30 where the FCT limiter is ill-conditioned.
     Returns (h [nC][L], hEdge [nE][L], u [nE][L], tracers [nC][L][T]).
     """
     rng = np.random.default_rng(seed)
@@ -152,5 +154,6 @@ def ocean_state(mesh, seed, nlev=60, ntr=3, layer_thickness=None, u_peak=0.3, de
         for t in range(3, ntr):
             q = field_c()
             tr[:, k, t] = (q - q.min()) / (q.max() - q.min())
-    tr[:, :, 0] = np.clip(tr[:, :, 0], 0.0, 30.0) if ntr > 0 else tr[:, :, 0]
+    if ntr > 0 and clip:
+        tr[:, :, 0] = np.clip(tr[:, :, 0], 0.0, 30.0)
     return h, hE, u, tr

@@ -199,3 +199,26 @@ def test_history_snapshots_while_stepping():
     st.snapshot_wait()
     for (hp, tp), (h, tr) in zip(snaps, want):
         assert np.array_equal(hp.numpy(), h) and np.array_equal(tp.numpy(), tr)
+
+
+def test_ocean_without_fct_mixes_but_does_not_advect():
+    """The ocean app advects tracers only through FCT (apps/ocean/run.cc:20-38):
+    with fct = 0 and del2 mixing on, a nonzero velocity leaves only the mixing."""
+    import mpaso.gpu as G
+    from mpaso.initial import ocean_state
+    mesh = mpaso.Mesh.icosa(3)
+    L, T, dt = 2, 2, 600.0
+    S = Oracle("restatement")
+    f = S.fct_statics(mesh, L)
+    h, hE, u, tr = ocean_state(mesh, 5, L, T, clip=False)
+    cfg = S.config(L, T, hmix=True, kappa=1e5)
+    want1 = S.ocean_run(mesh, S.static(mesh, f), cfg, dt, 1, h, hE, u, tr)
+    want20 = S.ocean_run(mesh, S.static(mesh, f), cfg, dt, 20, h, hE, u, tr)
+    dm = G.DeviceMesh(mesh, fct=f)
+    st = G.State(dm, app=G.APP_OCEAN, nlev=L, ntr=T, hmix=True, kappa=1e5)
+    for fld, a in ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr), (G.FIELD_LAYER_THICKNESS_EDGE, hE)):
+        st.set(fld, a)
+    st.step_graph(dt, 1)
+    assert rel_max(st.get(G.FIELD_TRACERS), want1) < TOL1
+    st.step_graph(dt, 19)
+    assert rel_max(st.get(G.FIELD_TRACERS), want20) < TOL100
