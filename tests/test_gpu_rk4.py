@@ -222,3 +222,40 @@ def test_ocean_without_fct_mixes_but_does_not_advect():
     assert rel_max(st.get(G.FIELD_TRACERS), want1) < TOL1
     st.step_graph(dt, 19)
     assert rel_max(st.get(G.FIELD_TRACERS), want20) < TOL100
+
+
+@pytest.mark.parametrize("app,opts", [
+    ("sw", dict(fct=True)), ("sw", dict(hmix=True, kappa=1e5)), ("sw", dict(fct=True, nu=1e5)),
+    ("sw", dict(hmix=True, kappa=1e5, nu=1e5)),
+    ("ocean", dict(fct=True)), ("ocean", dict()), ("ocean", dict(fct=True, hmix=True, kappa=1e5))])
+def test_every_option_combination_against_oracle(app, opts):
+    """Each combination of FCT advection, del2 tracer mixing and del2 momentum the
+    two apps accept, on the fused path against the oracle after 1 and 10 steps."""
+    import mpaso.gpu as G
+    from mpaso.initial import ocean_state
+    mesh = mpaso.Mesh.icosa(3)
+    L, T, dt, n = 2, 2, 450.0, 10
+    S = Oracle("restatement")
+    f = S.fct_statics(mesh, L)
+    cfg = S.config(L, T, **opts)
+    dm = G.DeviceMesh(mesh, fct=f)
+    if app == "sw":
+        h, u, tr = sw_state(mesh, 21, L, T)
+        run = lambda k: S.sw_run(mesh, S.static(mesh, f), cfg, dt, k, h, u, tr)  # noqa: E731
+        st = G.State(dm, nlev=L, ntr=T, **opts)
+        fields = ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr))
+        out = (G.FIELD_H, G.FIELD_U, G.FIELD_TRACERS)
+    else:
+        h, hE, u, tr = ocean_state(mesh, 21, L, T, clip=False)
+        run = lambda k: (S.ocean_run(mesh, S.static(mesh, f), cfg, dt, k, h, hE, u, tr),)  # noqa: E731
+        st = G.State(dm, app=G.APP_OCEAN, nlev=L, ntr=T, **opts)
+        fields = ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr), (G.FIELD_LAYER_THICKNESS_EDGE, hE))
+        out = (G.FIELD_TRACERS,)
+    for fld, a in fields:
+        st.set(fld, a)
+    st.step_graph(dt, 1)
+    for fld, want in zip(out, run(1)):
+        assert rel_max(st.get(fld), want) < TOL1
+    st.step_graph(dt, n - 1)
+    for fld, want in zip(out, run(n)):
+        assert rel_max(st.get(fld), want) < TOL100
