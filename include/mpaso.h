@@ -58,7 +58,11 @@ typedef struct {
   const double *bottomDepth;   /* h_s of the sw app; NULL = 0 */
   /* cell centres: used only to build the Hilbert ordering; NULL = keep order */
   const double *xCell, *yCell, *zCell;
-  int32_t reorder; /* 1 = renumber along a Hilbert curve, 0 = keep numbering */
+  /* renumbering: 0 keep the numbering; 1 cells along a Hilbert curve, edges and
+   * vertices after their cells; 2 cells, edges and vertices each along the
+   * Hilbert curve of their own position; 3 cells in Morton order, edges and
+   * vertices after their cells (results agree across orders to rounding) */
+  int32_t reorder;
   /* FCT / del2 statics (apps/ocean/state.hh:261-294); NULL = not available */
   int32_t fct_nlev; /* level count of highOrderAdvMask */
   const int32_t *maxLevelCell, *maxLevelEdgeTop, *nAdvCellsForEdge;

@@ -38,6 +38,13 @@ uint64_t hilbert_key(const uint32_t *coords, int dims, int bits) {
   return key;
 }
 
+uint64_t morton_key(const uint32_t *coords, int dims, int bits) {
+  uint64_t key = 0;
+  for (int b = bits - 1; b >= 0; --b)
+    for (int i = 0; i < dims; ++i) key = (key << 1) | ((coords[i] >> b) & 1u);
+  return key;
+}
+
 }  // namespace mpaso
 
 extern "C" const char *mpaso_last_error(void) { return mpaso::g_last_error.c_str(); }

@@ -46,5 +46,7 @@ template <class F> int guarded(const char *where, F &&body) {
 // `bits` bits.  Transpose-form algorithm of J. Skilling, "Programming the
 // Hilbert curve", AIP Conf. Proc. 707 (2004).
 uint64_t hilbert_key(const uint32_t *coords, int dims, int bits);
+// Morton (Z-order) index: the coordinates' bits interleaved, most significant first.
+uint64_t morton_key(const uint32_t *coords, int dims, int bits);
 
 }  // namespace mpaso

@@ -133,31 +133,56 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   for (int64_t e = 0; e < nE; ++e) maxEoE = std::max(maxEoE, (int)e2e.len(e));
 
   // ---- permutation ----
+  // reorder: 0 keep the numbering; 1 cells along a Hilbert curve, edges and
+  // vertices after the lowest new id of their cells; 2 cells, edges and
+  // vertices each along the Hilbert curve of their own position (edge:
+  // midpoint of its cells, vertex: centroid of its cells); 3 cells in Morton
+  // (Z) order, edges and vertices as in 1.  Each ensemble member is ordered
+  // inside its own block.
+  require(d.reorder >= 0 && d.reorder <= 3, MPASO_ERR_ARG, "reorder must be 0..3");
   std::vector<int32_t> pc(nC), pe(nE), pv(nV);
   std::iota(pc.begin(), pc.end(), 0);
+  std::iota(pe.begin(), pe.end(), 0);
+  std::iota(pv.begin(), pv.end(), 0);
+  std::vector<int32_t> member(nC, 0);
+  struct Box {
+    double lo[3], hi[3];
+    int dims, bits;
+  };
+  std::vector<Box> boxes;
+  const double *xyz[3] = {d.xCell, d.yCell, d.zCell};
+  auto quant = [&](const Box &B, const double *p, uint32_t q[3]) {
+    for (int a = 0; a < 3; ++a) q[a] = 0;
+    for (int a = 0; a < B.dims; ++a) {
+      const double span = B.hi[a] > B.lo[a] ? B.hi[a] - B.lo[a] : 1.0;
+      const double t = std::min(1.0, std::max(0.0, (p[a] - B.lo[a]) / span));
+      q[a] = (uint32_t)(t * (double)((1u << B.bits) - 1));
+    }
+  };
+  auto cell_pos = [&](int64_t c, double p[3]) {
+    for (int a = 0; a < 3; ++a) p[a] = xyz[a] ? xyz[a][c] : 0.0;
+  };
   if (d.reorder) {
     require(d.xCell && d.yCell, MPASO_ERR_ARG, "reorder needs xCell/yCell(/zCell)");
-    const double *xyz[3] = {d.xCell, d.yCell, d.zCell};
     const std::vector<int64_t> whole = {0, nC};
     const std::vector<int64_t> &blk = mcells ? *mcells : whole;
     std::vector<uint64_t> key(nC);
-    std::vector<int32_t> member(nC, 0);
     for (size_t b = 0; b + 1 < blk.size(); ++b) {
       const int64_t c0 = blk[b], c1 = blk[b + 1];
-      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      Box B{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}, 2, 30};
       for (int a = 0; a < 3; ++a)
         if (xyz[a])
-          for (int64_t c = c0; c < c1; ++c) lo[a] = std::min(lo[a], xyz[a][c]), hi[a] = std::max(hi[a], xyz[a][c]);
+          for (int64_t c = c0; c < c1; ++c) B.lo[a] = std::min(B.lo[a], xyz[a][c]), B.hi[a] = std::max(B.hi[a], xyz[a][c]);
       // a member whose z is absent or constant (a plane) is ordered in 2-D
-      const int dims = (d.zCell && hi[2] > lo[2]) ? 3 : 2;
-      const int bits = dims == 3 ? 20 : 30;
+      B.dims = (d.zCell && B.hi[2] > B.lo[2]) ? 3 : 2;
+      B.bits = B.dims == 3 ? 20 : 30;
+      boxes.push_back(B);
       for (int64_t c = c0; c < c1; ++c) {
-        uint32_t q[3] = {0, 0, 0};
-        for (int a = 0; a < dims; ++a) {
-          const double span = hi[a] > lo[a] ? hi[a] - lo[a] : 1.0;
-          q[a] = (uint32_t)((xyz[a][c] - lo[a]) / span * (double)((1u << bits) - 1));
-        }
-        key[c] = hilbert_key(q, dims, bits);
+        double p[3];
+        uint32_t q[3];
+        cell_pos(c, p);
+        quant(B, p, q);
+        key[c] = d.reorder == 3 ? morton_key(q, B.dims, B.bits) : hilbert_key(q, B.dims, B.bits);
         member[c] = (int32_t)b;
       }
     }
@@ -167,9 +192,31 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   }
   std::vector<int32_t> ic(nC);
   for (int64_t k = 0; k < nC; ++k) ic[pc[k]] = (int32_t)k;
-  std::iota(pe.begin(), pe.end(), 0);
-  std::iota(pv.begin(), pv.end(), 0);
-  if (d.reorder) {
+  if (d.reorder == 2) {  // edges and vertices on their own curves, inside their member's block
+    auto own_key = [&](const int32_t *cells, int n) {
+      double p[3] = {0, 0, 0}, q[3];
+      for (int j = 0; j < n; ++j) {
+        cell_pos(cells[j], q);
+        for (int a = 0; a < 3; ++a) p[a] += q[a] / n;
+      }
+      uint32_t u[3];
+      const Box &B = boxes[member[cells[0]]];
+      quant(B, p, u);
+      return std::make_pair(member[cells[0]], hilbert_key(u, B.dims, B.bits));
+    };
+    std::vector<std::pair<int32_t, uint64_t>> ek(nE), vk(nV);
+    for (int64_t e = 0; e < nE; ++e) {
+      const int32_t cs[2] = {e2c.at(e, 0), e2c.at(e, 1)};
+      ek[e] = own_key(cs, 2);
+    }
+    for (int64_t v = 0; v < nV; ++v) {
+      int32_t cs[kVertexDegree];
+      for (int j = 0; j < kVertexDegree; ++j) cs[j] = v2c.at(v, j);
+      vk[v] = own_key(cs, kVertexDegree);
+    }
+    std::stable_sort(pe.begin(), pe.end(), [&](int32_t a, int32_t b) { return ek[a] < ek[b]; });
+    std::stable_sort(pv.begin(), pv.end(), [&](int32_t a, int32_t b) { return vk[a] < vk[b]; });
+  } else if (d.reorder) {
     auto ekey = [&](int32_t e) {
       const int32_t a = ic[e2c.at(e, 0)], b = ic[e2c.at(e, 1)];
       return std::make_pair(std::min(a, b), std::max(a, b));

@@ -95,7 +95,7 @@ def _mesh_desc(mesh, fct, bottomDepth, reorder, keep):
         setattr(d, n, arr(f[n], np.float64))
     if bottomDepth is not None:
         d.bottomDepth = arr(bottomDepth, np.float64)
-    d.reorder = 1 if reorder else 0
+    d.reorder = int(reorder)  # True -> 1 (Hilbert), False -> 0, or an explicit mode 0..3
     if fct is not None:
         d.fct_nlev = fct["highOrderAdvMask"].shape[1]
         for n in ("maxLevelCell", "maxLevelEdgeTop", "nAdvCellsForEdge", "advCellsForEdge",
@@ -356,3 +356,44 @@ class State:
         b = ctypes.c_int64()
         check(lib().mpaso_state_device_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+
+# ---------------------------------------------------------------- ordering tuner
+ORDERINGS = {0: "file order", 1: "Hilbert cells, edges/vertices after their cells",
+             2: "Hilbert curve per entity (cells, edge midpoints, vertex centroids)",
+             3: "Morton cells, edges/vertices after their cells"}
+
+
+def tune_ordering(mesh, fields, dt, fct=None, bottomDepth=None, state_kwargs=None, nsteps=50,
+                  modes=(1, 2, 3, 0), device=0):
+    """The ordering half of the per-mesh autotuner: builds the device mesh in each
+    numbering of `modes`, autotunes the state's launch configuration on it
+    (State.autotune) and times `nsteps` graph-replayed steps; returns
+    (best mode, {mode: ms per step}, (DeviceMesh, State) of the best mode, its
+    launch configuration).  `fields` maps FIELD_* ids to arrays in the reference
+    numbering; the returned state holds them, unstepped."""
+    import time
+    state_kwargs = dict(state_kwargs or {})
+    ms, best = {}, None
+    for mode in modes:
+        dm = DeviceMesh(mesh, fct=fct, bottomDepth=bottomDepth, reorder=mode, device=device)
+        st = State(dm, **state_kwargs)
+        for f, a in fields.items():
+            st.set(f, a)
+        cfg = st.autotune(dt, 3)
+        st.step_graph(dt, 2)  # capture + warm-up
+        st.sync()
+        t0 = time.perf_counter()
+        st.step_graph(dt, nsteps)
+        st.sync()
+        ms[mode] = (time.perf_counter() - t0) * 1e3 / nsteps
+        if best is None or ms[mode] < ms[best[0]]:
+            if best is not None:
+                best[1].close(), best[2].close()
+            best = (mode, st, dm, cfg)
+        else:
+            st.close(), dm.close()
+    mode, st, dm, cfg = best
+    for f, a in fields.items():  # back to the initial fields
+        st.set(f, a)
+    return mode, ms, (dm, st), cfg
