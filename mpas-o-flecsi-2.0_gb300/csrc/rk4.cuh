@@ -308,9 +308,13 @@ __device__ __forceinline__ void cell_limiter(const DMesh &m, const Stage &S, int
       mx[t] = dmax(mx[t], x);
       mn[t] = dmin(mn[t], x);
       tl[t] += dmask(dflip(S.LO[ie0 + t], sm), ok);
-      const double ax = dflip(S.A[ie0 + t], sm);
-      fi[t] += dmask(dpos(ax), ok);
-      fo[t] += dmask(dneg(ax), ok);
+      // flxIn gets the positive signed fluxes, flxOut the others: one add into
+      // the accumulator the sign selects (integer-pipe select, same sums)
+      const double ax = dmask(dflip(S.A[ie0 + t], sm), ok);
+      const bool in = dgt0(ax);
+      const double acc = (in ? fi[t] : fo[t]) + ax;
+      fi[t] = in ? acc : fi[t];
+      fo[t] = in ? fo[t] : acc;
     }
   });
   const double dtia = S.dt * m.invAreaCell[c];  // dt / area
