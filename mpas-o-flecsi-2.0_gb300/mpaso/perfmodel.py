@@ -74,9 +74,10 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
         b2 += 8 * slot_c
         if fct:
             b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
-            # 1/hProv (5), dt/area, dt/(area hProv); per tracer 3 sums per edge, trUp (3),
-            # numerators / denominators (4), two guarded quotients (10, a quarter of the cells)
-            f2 += cl * (7 + T * (3 * Nc + 7 + 2.5))
+            # 1/hProv (5), dt/area, dt/(area hProv); per tracer 2 sums per edge (the upwind
+            # sum, and flxIn or flxOut by the flux sign), trUp (3), numerators / denominators
+            # (4), two guarded quotients (10, a quarter of the cells)
+            f2 += cl * (7 + T * (2 * Nc + 7 + 2.5))
         else:
             b2 += 8 * el * T + 8 * cl * T
             f2 += cl * T * Nc
@@ -115,7 +116,7 @@ def ocean_kernels(d: Dims, fct=True, hmix=True):
         f1 += el * (1 + 2 * T)
     b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
     b2 += 16 * el * T + 24 * cl * T
-    f2 = cl * (2 + T * (3 * Nc + 7 + 2.5))
+    f2 = cl * (2 + T * (2 * Nc + 7 + 2.5))
     b3 = 4 * nC + 12 * slot_c + 8 * nC + 8 * nE + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
     b3 += 8 * el * T * (int(fct) + int(hmix))
     f3 = cl * T * (Nc * (1 + int(fct)) + 2.75)
