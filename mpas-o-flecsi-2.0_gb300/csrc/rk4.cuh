@@ -228,14 +228,12 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
       for (int t = 0; t < T; ++t) s[t] = fma(cf, tr[t], s[t]);
     }
     const int mask = m.hoMask[(int64_t)e * m.fctLev + k];
-    const double wgt = mask ? F : 0.0;
 #pragma unroll
     for (int t = 0; t < T; ++t) {
       const double lo = dvF * (up1 ? t1[t] : t2[t]);
-      double ho = wgt * s[t];
-      if (!mask) ho = fma(0.5 * dvF, t1[t] + t2[t], ho);  // solve.cc:222-225
       S.LO[i * T + t] = lo;
-      S.A[i * T + t] = ho - lo;
+      // A = HO - LO, HO = F s (masked edges: the centred flux, solve.cc:222-225)
+      S.A[i * T + t] = mask ? fma(F, s[t], -lo) : fma(0.5 * dvF, t1[t] + t2[t], -lo);
     }
   } else if (S.centred) {
     // centred flux of compute_scalar_tend (apps/sw/tasks/solve.cc:255-269)
@@ -373,9 +371,10 @@ __device__ __forceinline__ void cell_tracer_tend(const DMesh &m, const Stage &S,
         const double a = S.A[ie0 + t];
         const double2 o = S.R2[jn + t];
         const double r = dgt0(a) == own_first ? dmin(own[t].y, o.x) : dmin(o.y, own[t].x);
-        x = a * r;
+        x = S.hmix ? fma(a, r, -S.DF[ie0 + t]) : a * r;  // limited flux - del2 flux in one FMA
+      } else if (S.hmix) {
+        x = -S.DF[ie0 + t];
       }
-      if (S.hmix) x -= S.DF[ie0 + t];
       tend[t] += dmask(dflip(x, sm), ok);
     }
   });
