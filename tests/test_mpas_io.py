@@ -197,3 +197,4 @@ def test_mpas_mesh_written_elsewhere_with_narrower_columns(tmp_path):
         g.put_var("edgesOnCell", np.ones((2, 9), np.int32))
     with pytest.raises(ValueError):
         read_mesh(wide)
+
