@@ -495,7 +495,7 @@ def ensemble_arm(args):
     mfct = [fct_statics(m, 1) for m in members]
     states = [sw_state(m, 5000 + i, 1, 1) for i, m in zip(mine, members)]
     opts = dict(fct=True, hmix=True, kappa=1e3, nu=1e3)
-    dt, K, W = 30.0, args.steps, args.warmup
+    dt, K, W = 30.0, min(args.steps, 200), args.warmup  # the ensemble workload is 200 steps
     dm = G.DeviceMesh.ensemble(members, mfct, device=local)
     log(f"ensemble built in {time.time() - t0:.1f}s: {len(members)} members, {dm.nC} cells on rank {rank}")
     st = G.State(dm, nlev=1, ntr=1, **opts)
