@@ -374,6 +374,8 @@ def adjoint_arm(args):
         errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
     mem = dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes()
     tracers = adjoint_tracer_leg(args, mesh, N, K, dt)
+    del st, dm
+    ocean = ocean_adjoint_leg(args)
     return {"metric": "adjoint/forward time ratio (sw RK4, level-6 sphere)",
             "value": t_vjp / t_fwd, "unit": "ratio", "higher_is_better": False, "n_gpus": 1,
             "steps": N, "dtype": "f64", "data": "synthetic (seeded smooth fields)",
@@ -384,7 +386,7 @@ def adjoint_arm(args):
             "vjp_over_plain_forward": t_vjp / t_plain,
             "fd_check": {"directions": args.adj_dirs, "max_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None},
-            "peak_device_bytes": int(mem), "stored_window": stored, "tracers": tracers}
+            "peak_device_bytes": int(mem), "stored_window": stored, "tracers": tracers, "ocean_tracers": ocean}
 
 
 def adjoint_tracer_leg(args, mesh, N, K, dt):
@@ -460,6 +462,86 @@ def adjoint_tracer_leg(args, mesh, N, K, dt):
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
             "vjp_over_plain_forward": t_vjp / t_plain, "stored_window": stored,
             "fd_check": {"directions": len(errs), "max_rel_err": max(errs) if errs else None},
+            "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
+
+
+def ocean_adjoint_leg(args, N=20, K=10):
+    """The ocean app's tracers (level-6 sphere, 60 levels x 3 tracers, FCT +
+    del2, dt = 450 s, unclipped temperature; thickness and velocity prescribed): J = 1/2 <area
+    (tr_N - tr_target)^2> / sum(area), gradient w.r.t. tr0 through
+    mpaso_rk4_vjp_tracers, checkpoints every K of N steps, timed against the
+    forward of the same state."""
+    import numpy as np
+    import torch
+
+    import mpaso
+    import mpaso.gpu as G
+    from mpaso.initial import ocean_state
+    from mpaso.setup import fct_statics
+    cfg = CONFIGS["ocean_l6"]
+    mesh = mpaso.Mesh.icosa(cfg["level"])
+    fct = fct_statics(mesh, cfg["L"])
+    # temperature not clipped to [0, 30]: on clipped plateaus the limiter's
+    # quotients divide rounding-level differences by its 1e-10 regulariser and
+    # no difference quotient can check the branch derivative
+    h, hE, u, tr0 = ocean_state(mesh, 1234, cfg["L"], cfg["T"], clip=False)
+    trt = tr0[::-1].copy()
+    w = (mesh.fields["areaCell"] / mesh.fields["areaCell"].sum())[:, None, None]
+    dm = G.DeviceMesh(mesh, fct=fct)
+    st = G.State(dm, app=G.APP_OCEAN, nlev=cfg["L"], ntr=cfg["T"], fct=True, hmix=True, kappa=cfg["kappa"])
+    for f, a in ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_LAYER_THICKNESS_EDGE, hE)):
+        st.set(f, a)
+    ext = torch.cuda.ExternalStream(st.stream())
+    dt = cfg["dt"]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        fn()
+        e1.record(ext)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    def final(tr):
+        st.set(G.FIELD_TRACERS, tr)
+        st.step(dt, N)
+        return st.get(G.FIELD_TRACERS)
+
+    zh, zu = np.zeros_like(h), np.zeros_like(u)
+    st.set(G.FIELD_TRACERS, tr0)
+    st.forward(dt, N, K)
+    st.vjp_tracers(zh, zu, np.zeros_like(tr0))
+    st.set(G.FIELD_TRACERS, tr0)
+    st.step_graph(dt, 2)
+    st.set(G.FIELD_TRACERS, tr0)
+    t_plain = timed(lambda: st.step_graph(dt, N))
+    st.set(G.FIELD_TRACERS, tr0)
+    t_fwd = timed(lambda: st.forward(dt, N, K))
+    g_N = w * (st.get(G.FIELD_TRACERS) - trt)
+    out = {}
+    t_vjp = timed(lambda: out.update(g=st.vjp_tracers(zh, zu, g_N)))
+    gt = out["g"][2]
+    # central differences along random directions at two perturbation sizes:
+    # the FCT limiter's quotients (regularised by 1e-10) change branch under
+    # larger perturbations, so the difference quotient approaches the branch
+    # derivative only as the perturbation shrinks.  J(+) - J(-) is summed as
+    # sum w (a+ - a-)(a+ + a- - 2 target) / 2, each cell's difference taken
+    # before the sum (the sum of squares itself cancels to ~1e-11).
+    rng = np.random.default_rng(8)
+    fd_rows = []
+    for _ in range(min(args.adj_dirs, 2)):
+        v = rng.standard_normal(tr0.shape)
+        ad = float((gt * v).sum())
+        for d in (1e-6, 1e-8, 1e-10):
+            ap, am = final(tr0 + d * v), final(tr0 - d * v)
+            fd = float((w * (ap - am) * (ap + am - 2.0 * trt)).sum()) / (4 * d)
+            fd_rows.append({"perturbation": d, "fd": fd, "ad": ad, "rel_err": abs(fd - ad) / max(abs(ad), 1e-300)})
+    return {"workload": f"{cfg['workload']}, {N} steps, dt={dt}s, checkpoint every {K}, loss on the final tracers",
+            "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
+            "vjp_over_plain_forward": t_vjp / t_plain,
+            "fd_check": fd_rows,
+            "adjoint_device_bytes": int(st.adjoint_device_bytes()),
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
 
 

@@ -289,9 +289,12 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
  * configuration (12 ints).  Call it outside stream capture. */
 int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config);
 
-/* Adjoint of the sw RK4 step.  No counterpart in the reference, which has no
+/* Adjoint of the RK4 step.  No counterpart in the reference, which has no
  * adjoint: these differentiate what mpaso_rk4_step computes for app =
- * MPASO_APP_SW (apps/sw/run.cc:10-60) with pin_u = 0.
+ * MPASO_APP_SW (apps/sw/run.cc:10-60) with pin_u = 0, and, through
+ * mpaso_rk4_vjp_tracers, the tracers of app = MPASO_APP_OCEAN
+ * (apps/ocean/run.cc:10-50), whose thickness and velocity are prescribed
+ * inputs: there gh / gu may be NULL and gh0 / gu0 (when given) receive zeros.
  *
  * mpaso_rk4_forward: advances the state nsteps steps of size dt like
  * mpaso_rk4_step, keeping a checkpoint of (h, u, tracers) every ckpt_every

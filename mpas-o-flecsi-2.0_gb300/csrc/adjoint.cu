@@ -148,7 +148,9 @@ struct TrArgs {
   int2 *amm;                       // cells holding the {max, min} bound
   double *muh_t, *lFt, *lhet;
   double2 *p12, *lho;              // per edge and tracer: parts for cells(e); lambda_HO F by sign of F
-  int T, rk, fct, hmix;
+  const double *Fx, *hEx;          // ocean: the prescribed thickness flux and edge thickness
+  int T, rk, fct, hmix, ocean;     // ocean: tracers only, h / u prescribed, no q = h tr
+  int centred;                     // without FCT: the sw app's centred flux (1) or no advection (0, ocean)
   double dt;
 };
 
@@ -434,7 +436,7 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
     lhpi = fma(lup, num, lhpi);
     lhpi = fma(fma(ldp, fi, -ldm * fo), dtia, lhpi);
   }
-  if (lane) return;
+  if (lane || a.ocean) return;  // ocean: h and the thickness flux are prescribed
   // hProv = h + dt tend_h: its cotangent goes to h and to the thickness tendency
   const double lhp = -lhpi * hpi * hpi;
   a.muh_t[i] = lh + lhp;
@@ -447,8 +449,9 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
 // tracer, or dv (tr1 + tr2) / 2 where the high-order mask is 0) give F and
 // the tracers (solve.cc:99-167, 216-229).  S is read back as HO / F = (A +
 // LO) / F from the taped fluxes (the stencil is summed only where F = 0).
-// Without FCT: the centred flux of apps/sw/tasks/solve.cc:237-270.  del2
-// mixing (ocean solve.cc:328-366) adds to h_e and the tracers.  Per edge and
+// Without FCT: the centred flux of apps/sw/tasks/solve.cc:237-270 (sw) or no
+// advection (ocean, whose advection is the FCT task alone).  del2 mixing
+// (ocean solve.cc:328-366) adds to h_e and the tracers.  Per edge and
 // tracer the parts for cells(e) go to p12 and lambda_HO F, split by the sign
 // of F, to lho (TC gathers them); per edge the thickness-flux and
 // edge-thickness cotangents summed over tracers go to lFt / lhet (B1 adds them).
@@ -458,7 +461,8 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L), T = a.T;
   const int2 c = m.coe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-  const double he = 0.5 * (a.h[i1] + a.h[i2]), F = a.u[i] * he, dv = m.dvEdge[e];
+  const double he = a.ocean ? a.hEx[i] : 0.5 * (a.h[i1] + a.h[i2]);
+  const double F = a.ocean ? a.Fx[i] : a.u[i] * he, dv = m.dvEdge[e];
   const bool pos = dgt0(F), neg = dlt0(F);
   const int mask = a.fct ? m.hoMask[(int64_t)e * m.fctLev + k] : 0;
   const double kd = a.hmix ? a.kd[e] : 0.0;
@@ -508,7 +512,7 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
         p1 += q, p2 += q;
         a.lho[it] = make_double2(0.0, 0.0);
       }
-    } else {
+    } else if (a.centred) {
       const double hd = 0.5 * dv;
       lF = fma(G * hd, tr1 + tr2, lF);
       p1 = p2 = G * hd * F;
@@ -520,6 +524,7 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
     }
     a.p12[it] = make_double2(p1, p2);
   }
+  if (a.ocean) return;
   a.lFt[i] = lF;
   a.lhet[i] = lhe;
 }
@@ -539,8 +544,8 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
   const int64_t i = g / NL;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c], T = a.T;
-  const double hinv = rcp_nr(a.h[i]), inva = m.invAreaCell[c];
-  double mh = a.fct ? a.muh_t[i] : 0.0;
+  const double hinv = a.ocean ? 1.0 : rcp_nr(a.h[i]), inva = m.invAreaCell[c];
+  double mh = a.fct && !a.ocean ? a.muh_t[i] : 0.0;
   for (int t = 0; t < T; ++t) {
     const int64_t it = i * T + t;
     double lt = 0.0;
@@ -587,11 +592,11 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
       if (am.x == c) lt += lb.x;
       if (am.y == c) lt += lb.y;
     }
-    const double mq = lt * hinv;  // tr = q / h
-    mh = fma(-mq, a.tr[it], mh);
+    const double mq = lt * hinv;  // sw: tr = q / h; ocean: the state is tr itself
+    if (!a.ocean) mh = fma(-mq, a.tr[it], mh);
     a.gq[it] = combine(a.rk, a.dt, it, mq, a.lam_q, a.acc_q, a.lk_q) * inva;
   }
-  if (lane == 0) a.muh_t[i] = mh;
+  if (lane == 0 && !a.ocean) a.muh_t[i] = mh;
 }
 
 // Window ends: lambda_q = lambda_tr / h, lambda_h -= sum_t lambda_tr tr / h
@@ -638,22 +643,25 @@ void ensure_buffers(SwState &s, int N, int k) {
   if (A && A->cap_ck >= nck && A->cap_k >= k) return;
   free_adjoint(s);
   A = s.adj = new AdjBuffers();
+  // the ocean app differentiates its tracers only: no (h, u) tape or cotangents
+  const int64_t hu = s.p.app == MPASO_APP_OCEAN ? 0 : 1;
   std::vector<std::pair<double **, int64_t>> bufs = {
-      {&A->ck_u, nck * eu}, {&A->ck_h, nck * ch}, {&A->tp_u, (4LL * k + 1) * eu},
-      {&A->tp_h, (4LL * k + 1) * ch}, {&A->uacc, eu}, {&A->hacc, ch}, {&A->tp_pv, (4LL * k + 1) * vv},
-      {&A->tp_hs, (4LL * k + 1) * vv}, {&A->tp_s1, 4LL * k * eu},
-      {(double **)&A->FP, 2 * eu}, {&A->pve, eu}, {&A->lam_u, eu}, {&A->lam_h, ch}, {&A->acc_u, eu},
-      {&A->acc_h, ch}, {&A->lk_u, eu}, {&A->lk_h, ch}, {&A->mu_u, eu}, {&A->mu_h, ch}, {&A->lhe, eu},
-      {&A->lpve, eu}, {&A->lke, ch}, {&A->ldiv, ch}, {&A->lcirc, vv}, {&A->lhs, vv}};
+      {&A->ck_u, hu * nck * eu}, {&A->ck_h, hu * nck * ch}, {&A->tp_u, hu * (4LL * k + 1) * eu},
+      {&A->tp_h, hu * (4LL * k + 1) * ch}, {&A->uacc, hu * eu}, {&A->hacc, hu * ch},
+      {&A->tp_pv, hu * (4LL * k + 1) * vv}, {&A->tp_hs, hu * (4LL * k + 1) * vv}, {&A->tp_s1, hu * 4LL * k * eu},
+      {(double **)&A->FP, hu * 2 * eu}, {&A->pve, hu * eu}, {&A->lam_u, hu * eu}, {&A->lam_h, hu * ch},
+      {&A->acc_u, hu * eu}, {&A->acc_h, hu * ch}, {&A->lk_u, hu * eu}, {&A->lk_h, hu * ch}, {&A->mu_u, hu * eu},
+      {&A->mu_h, hu * ch}, {&A->lhe, hu * eu}, {&A->lpve, hu * eu}, {&A->lke, hu * ch}, {&A->ldiv, hu * ch},
+      {&A->lcirc, hu * vv}, {&A->lhs, hu * vv}};
   if (s.T > 0) {
     const int64_t cT = ch * s.T, eT = eu * s.T;
     const std::vector<std::pair<double **, int64_t>> tb = {
         {&A->ck_tr, nck * cT}, {&A->tp_tr, (4LL * k + 1) * cT}, {&A->tp_A, 4LL * k * eT},
         {&A->tp_LO, 4LL * k * eT}, {(double **)&A->tp_R2, 8LL * k * cT}, {&A->tp_tLO, 4LL * k * cT},
-        {&A->tp_hpi, 4LL * k * ch}, {&A->trhacc, cT}, {&A->lam_q, cT}, {&A->acc_q, cT}, {&A->lk_q, cT},
+        {&A->tp_hpi, hu * 4LL * k * ch}, {&A->trhacc, cT}, {&A->lam_q, cT}, {&A->acc_q, cT}, {&A->lk_q, cT},
         {&A->gq, cT}, {&A->ltl, cT}, {&A->ltrs, cT}, {(double **)&A->lfio, 2 * cT},
-        {(double **)&A->lmm, 2 * cT}, {(double **)&A->amm, cT}, {&A->muh_t, ch}, {&A->lFt, eu},
-        {&A->lhet, eu}, {(double **)&A->lho, 2 * eT}, {(double **)&A->p12, 2 * eT}};
+        {(double **)&A->lmm, 2 * cT}, {(double **)&A->amm, cT}, {&A->muh_t, hu * ch}, {&A->lFt, hu * eu},
+        {&A->lhet, hu * eu}, {(double **)&A->lho, 2 * eT}, {(double **)&A->p12, 2 * eT}};
     bufs.insert(bufs.end(), tb.begin(), tb.end());
   }
   size_t total = 0;
@@ -696,17 +704,22 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
   }
   // plain stream order: programmatic dependent launch made this 25% slower (measured)
   const bool pdl = false;
-  if (first) launch_pdl(k_adj_prep, nE, TPB, pdl, st, m, a, L);
+  const bool ocean = s.p.app == MPASO_APP_OCEAN;
+  if (first && !ocean) launch_pdl(k_adj_prep, nE, TPB, pdl, st, m, a, L);
   if (A.tr) {
     const int64_t cT = nC * s.T, eT = nE * s.T;
     TrArgs t{};
     t.u = a.u, t.h = a.h, t.tr = A.tp_tr + (size_t)j * cT;
     t.A = A.tp_A + (size_t)j * eT, t.LO = A.tp_LO + (size_t)j * eT, t.R2 = A.tp_R2 + (size_t)j * cT;
     t.hpi = A.tp_hpi + (size_t)j * nC, t.tLO = A.tp_tLO + (size_t)j * cT;
+    if (ocean) {  // prescribed thickness, edge thickness, flux and 1/hProv
+      t.ocean = 1, t.h = s.H[0], t.hpi = s.HPI, t.Fx = s.F, t.hEx = s.HE;
+    }
     t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.gq = A.gq, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
     t.ltl = A.ltl, t.ltrs = A.ltrs, t.lfio = A.lfio, t.lmm = A.lmm, t.amm = A.amm;
     t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.p12 = A.p12, t.lho = A.lho;
     t.T = s.T, t.rk = rk, t.fct = s.p.fct ? 1 : 0, t.hmix = s.p.hmix ? 1 : 0, t.dt = A.dt;
+    t.centred = !t.fct && !t.ocean;
     constexpr int NLA = 1, NLC = 2;  // lanes per cell (measured best at level 6)
     if (t.fct) {
       if (m.maxEoC <= 6)
@@ -718,6 +731,7 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
     launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
     a.lFt = A.lFt, a.lhet = A.lhet, a.muh_t = A.muh_t;
   }
+  if (ocean) return;  // the ocean's h and u are prescribed: nothing more to reverse
   if (m.maxEoE == 10)
     launch_pdl(k_adj_b1<10>, nE, TPB, pdl, st, m, a, L);
   else
@@ -743,12 +757,18 @@ void forward_stored(SwState &s, double dt, int N) {
     cudaGraph_t g;
     MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     try {
-      MPASO_CUDA(cudaMemcpyAsync(A.tp_u, s.U[0], eu * 8, cudaMemcpyDeviceToDevice, s.stream));
-      MPASO_CUDA(cudaMemcpyAsync(A.tp_h, s.H[0], ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      const bool hu = s.p.app == MPASO_APP_SW;  // the ocean's h and u are prescribed
+      if (!hu) ocean_recompute(s, dt, s.stream);
+      if (hu) {
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_u, s.U[0], eu * 8, cudaMemcpyDeviceToDevice, s.stream));
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_h, s.H[0], ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      }
       if (with_tr) MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, s.TR0, ct * 8, cudaMemcpyDeviceToDevice, s.stream));
       tape_segment(s, A, N, with_tr, s.stream);
-      MPASO_CUDA(cudaMemcpyAsync(s.U[0], A.tp_u + 4 * (size_t)N * eu, eu * 8, cudaMemcpyDeviceToDevice, s.stream));
-      MPASO_CUDA(cudaMemcpyAsync(s.H[0], A.tp_h + 4 * (size_t)N * ch, ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      if (hu) {
+        MPASO_CUDA(cudaMemcpyAsync(s.U[0], A.tp_u + 4 * (size_t)N * eu, eu * 8, cudaMemcpyDeviceToDevice, s.stream));
+        MPASO_CUDA(cudaMemcpyAsync(s.H[0], A.tp_h + 4 * (size_t)N * ch, ch * 8, cudaMemcpyDeviceToDevice, s.stream));
+      }
       if (with_tr)
         MPASO_CUDA(cudaMemcpyAsync(s.TR0, A.tp_tr + 4 * (size_t)N * ct, ct * 8, cudaMemcpyDeviceToDevice, s.stream));
     } catch (...) {
@@ -768,7 +788,8 @@ void forward_stored(SwState &s, double dt, int N) {
 }
 
 void forward(SwState &s, double dt, int N, int k) {
-  require(s.p.app == MPASO_APP_SW, MPASO_ERR_ARG, "the adjoint covers the sw app");
+  const bool ocean = s.p.app == MPASO_APP_OCEAN;
+  require(!ocean || s.T > 0, MPASO_ERR_ARG, "the ocean app's adjoint differentiates its tracers: ntr >= 1");
   require(!s.p.pin_u, MPASO_ERR_ARG, "the adjoint does not support a pinned wind (test case 1)");
   require(N >= 1 && k >= 0, MPASO_ERR_ARG, "nsteps must be >= 1 and ckpt_every >= 0");
   const bool stored = k == 0;
@@ -785,17 +806,21 @@ void forward(SwState &s, double dt, int N, int k) {
   const DMesh &m = s.mesh->ctx.d;
   const size_t eu = (size_t)m.nE * s.L * 8, ch = (size_t)m.nC * s.L * 8;
   A.N = N, A.k = k, A.dt = dt, A.nck = (N + k - 1) / k;
-  MPASO_CUDA(cudaMemcpyAsync(A.ck_u, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
-  MPASO_CUDA(cudaMemcpyAsync(A.ck_h, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+  if (!ocean) {
+    MPASO_CUDA(cudaMemcpyAsync(A.ck_u, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
+    MPASO_CUDA(cudaMemcpyAsync(A.ck_h, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+  }
   const size_t ct = ch * s.T;
   if (s.T) MPASO_CUDA(cudaMemcpyAsync(A.ck_tr, s.TR0, ct, cudaMemcpyDeviceToDevice, s.stream));
   for (int done = 0, c = 1; done < N; ++c) {
     const int n = std::min(k, N - done);
     sw_steps_graph(s, dt, n);
     done += n;
-    if (done < N) {
+    if (done < N && !ocean) {
       MPASO_CUDA(cudaMemcpyAsync(A.ck_u + (size_t)c * m.nE * s.L, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
       MPASO_CUDA(cudaMemcpyAsync(A.ck_h + (size_t)c * m.nC * s.L, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+    }
+    if (done < N) {
       if (s.T)
         MPASO_CUDA(cudaMemcpyAsync(A.ck_tr + (size_t)c * m.nC * s.L * s.T, s.TR0, ct, cudaMemcpyDeviceToDevice,
                                    s.stream));
@@ -813,6 +838,22 @@ void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t s
   const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
   const int64_t cT = ch * s.T, eT = eu * s.T;
   const int64_t vv = (int64_t)m.nV * s.L;
+  if (s.p.app == MPASO_APP_OCEAN) {  // tracers only, over the prescribed flux and 1/hProv
+    for (int t = 0; t < n; ++t) {
+      double *ytr = A.tp_tr + (size_t)4 * t * cT;
+      for (int rk = 0; rk < 4; ++rk) {
+        const int j = 4 * t + rk;
+        Stage S = ocean_make_stage(s, rk, A.dt);
+        S.tr_in = ytr + (size_t)rk * cT, S.tr_prev = ytr;
+        S.tr_out = rk < 3 ? ytr + (size_t)(rk + 1) * cT : nullptr;
+        S.trh_acc = A.trhacc, S.tr_new = rk == 3 ? ytr + (size_t)4 * cT : nullptr;
+        S.A = A.tp_A + (size_t)j * eT, S.LO = A.tp_LO + (size_t)j * eT, S.R2 = A.tp_R2 + (size_t)j * cT;
+        S.tLO = A.tp_tLO + (size_t)j * cT;
+        ocean_launch_stage(s, S, st);
+      }
+    }
+    return;
+  }
   sw_diag_ptrs(s, A.tp_u, A.tp_h, A.tp_pv, A.tp_hs, st);
   for (int t = 0; t < n; ++t) {
     double *yu = A.tp_u + (size_t)4 * t * eu, *yh = A.tp_h + (size_t)4 * t * ch;
@@ -851,12 +892,16 @@ void reverse_body(SwState &s) {
   const int64_t eu = (int64_t)m.nE * s.L, ch = (int64_t)m.nC * s.L;
   const int64_t cT = ch * s.T;
   const cudaStream_t st = s.stream;
+  const bool ocean = s.p.app == MPASO_APP_OCEAN;
+  if (ocean) ocean_recompute(s, A.dt, st);  // the prescribed flux and 1/hProv the stages used
   for (int seg = A.nck - 1; seg >= 0; --seg) {
     const int s0 = seg * A.k, n = std::min(A.k, A.N - s0);
     if (!A.stored) {
       // taping recompute of the segment from its checkpoint
-      MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
-      MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
+      if (!ocean) {
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
+      }
       if (A.tr)
         MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, st));
       tape_segment(s, A, n, A.tr != 0, st);
@@ -864,11 +909,13 @@ void reverse_body(SwState &s) {
     if (seg == A.nck - 1) {
       // cotangents of the final state (tape slot 4n): tracers to q = h tr, then
       // the first reversed stage's lk = dt/6 lam
-      if (A.tr)
+      if (A.tr && !ocean)
         k_adj_q_convert<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, s.T, A.tp_h + (size_t)4 * n * ch,
                                                               A.tp_tr + (size_t)4 * n * cT, A.lam_q, A.lam_h, 0);
-      k_adj_init<<<blocks_for(eu, TPB), TPB, 0, st>>>(eu, A.lam_u, A.lk_u, A.dt / 6);
-      k_adj_init<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, A.lam_h, A.lk_h, A.dt / 6);
+      if (!ocean) {
+        k_adj_init<<<blocks_for(eu, TPB), TPB, 0, st>>>(eu, A.lam_u, A.lk_u, A.dt / 6);
+        k_adj_init<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, A.lam_h, A.lk_h, A.dt / 6);
+      }
       if (A.tr)
         k_adj_init_q<<<blocks_for(cT, TPB), TPB, 0, st>>>(m, s.L, s.T, A.lam_q, A.lk_q, A.gq, A.dt / 6);
     }
@@ -879,7 +926,7 @@ void reverse_body(SwState &s) {
       }
   }
   // q = h tr at the window's start (tape slot 0 holds checkpoint 0)
-  if (A.tr)
+  if (A.tr && !ocean)
     k_adj_q_convert<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, s.T, A.tp_h, A.tp_tr, A.lam_q, A.lam_h, 1);
   MPASO_CUDA(cudaGetLastError());
 }
@@ -959,6 +1006,8 @@ int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0
   return guarded("mpaso_rk4_vjp", [&] {
     require(s && gh && gu && gh0 && gu0, MPASO_ERR_ARG, "null argument");
     SwState &S = s->s;
+    require(S.p.app == MPASO_APP_SW, MPASO_ERR_ARG,
+            "the ocean app's thickness and velocity are prescribed: use mpaso_rk4_vjp_tracers");
     require(S.adj && S.adj->have_forward, MPASO_ERR_ARG, "mpaso_rk4_vjp needs a preceding mpaso_rk4_forward");
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);
@@ -974,8 +1023,10 @@ int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0
 int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, const double *gtr, double *gh0,
                           double *gu0, double *gtr0) {
   return guarded("mpaso_rk4_vjp_tracers", [&] {
-    require(s && gh && gu && gtr && gh0 && gu0 && gtr0, MPASO_ERR_ARG, "null argument");
+    require(s && gtr && gtr0, MPASO_ERR_ARG, "null argument");
     SwState &S = s->s;
+    const bool ocean = S.p.app == MPASO_APP_OCEAN;
+    require(ocean || (gh && gu && gh0 && gu0), MPASO_ERR_ARG, "null argument");
     require(S.T > 0, MPASO_ERR_ARG, "mpaso_rk4_vjp_tracers needs a state with tracers");
     require(S.adj && S.adj->have_forward, MPASO_ERR_ARG,
             "mpaso_rk4_vjp_tracers needs a preceding mpaso_rk4_forward");
@@ -983,13 +1034,26 @@ int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, con
     require(!S.adj->stored || S.adj->stored_tr, MPASO_ERR_ARG, "the stored window holds no tracers");
     MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
     const int64_t LT = (int64_t)S.L * S.T;
-    to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);
-    to_internal(S, gh, S.adj->lam_h, MPASO_CELLS, S.L);
+    if (!ocean) {
+      to_internal(S, gu, S.adj->lam_u, MPASO_EDGES, S.L);
+      to_internal(S, gh, S.adj->lam_h, MPASO_CELLS, S.L);
+    }
     to_internal(S, gtr, S.adj->lam_q, MPASO_CELLS, LT);
     S.adj->tr = 1;
     reverse(S);
-    from_internal(S, S.adj->lam_u, gu0, MPASO_EDGES, S.L);
-    from_internal(S, S.adj->lam_h, gh0, MPASO_CELLS, S.L);
+    if (!ocean) {
+      from_internal(S, S.adj->lam_u, gu0, MPASO_EDGES, S.L);
+      from_internal(S, S.adj->lam_h, gh0, MPASO_CELLS, S.L);
+    } else {  // prescribed fields: no cotangent is computed for them
+      const MeshCtx &ctx = S.mesh->ctx;
+      for (auto [p, n] : {std::make_pair(gh0, (int64_t)ctx.d.nC * S.L), std::make_pair(gu0, (int64_t)ctx.d.nE * S.L)}) {
+        if (!p) continue;
+        if (is_device_pointer(p))
+          MPASO_CUDA(cudaMemsetAsync(p, 0, (size_t)n * 8, S.stream));
+        else
+          std::memset(p, 0, (size_t)n * 8);
+      }
+    }
     from_internal(S, S.adj->lam_q, gtr0, MPASO_CELLS, LT);
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
   });

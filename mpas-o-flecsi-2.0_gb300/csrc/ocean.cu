@@ -175,4 +175,21 @@ void ocean_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
 
 int ocean_launches_per_step(const SwState &) { return 12; }
 
+// A stage with the state's weights and buffers, and its launch, for callers
+// that redirect some of its pointers (the adjoint's taping recompute).
+Stage ocean_make_stage(SwState &s, int rk, double dt) { return ocean_stage(s, rk, dt); }
+void ocean_launch_stage(SwState &s, const Stage &S, cudaStream_t st) {
+  switch (s.T) {
+    case 1: ocean_stage_T<1>(s, S, st); break;
+    case 2: ocean_stage_T<2>(s, S, st); break;
+    case 3: ocean_stage_T<3>(s, S, st); break;
+    case 4: ocean_stage_T<4>(s, S, st); break;
+    case 5: ocean_stage_T<5>(s, S, st); break;
+    case 6: ocean_stage_T<6>(s, S, st); break;
+    case 7: ocean_stage_T<7>(s, S, st); break;
+    case 8: ocean_stage_T<8>(s, S, st); break;
+    default: fail(MPASO_ERR_ARG, "ocean app needs 1..8 tracers");
+  }
+}
+
 }  // namespace mpaso

@@ -190,6 +190,9 @@ void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st);
 void sw_steps_graph(SwState &s, double dt, int nsteps);
 Stage sw_make_stage(SwState &s, int rk, double dt);
 void sw_launch_stage(SwState &s, const Stage &S, cudaStream_t st);
+Stage ocean_make_stage(SwState &s, int rk, double dt);
+void ocean_launch_stage(SwState &s, const Stage &S, cudaStream_t st);
+void ocean_recompute(SwState &s, double dt, cudaStream_t st);
 void drop_adjoint_graph(SwState &s);
 
 // ---------------------------------------------------------------------------

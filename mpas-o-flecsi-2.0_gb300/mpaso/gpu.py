@@ -333,7 +333,9 @@ class State:
 
     def vjp_tracers(self, gh, gu, gtr, out=None):
         """Cotangents of the initial (h, u, tracers) from cotangents of the final (h, u, tracers)
-        of the last forward; the FCT limiter is differentiated on the branch the forward took."""
+        of the last forward; the FCT limiter is differentiated on the branch the forward took.
+        On an ocean state h and u are prescribed: gh / gu are ignored and the returned
+        gh0 / gu0 are zero."""
         gh0, gu0, gtr0 = out if out is not None else (
             np.empty(self._shape(FIELD_H)), np.empty(self._shape(FIELD_U)), np.empty(self._shape(FIELD_TRACERS)))
         gh, gu, gtr = (np.ascontiguousarray(x, np.float64) if isinstance(x, np.ndarray) else x

@@ -122,11 +122,14 @@ class SwComplex:
             tend_u = tend_u + self.nu * ((div[c2] - div[c1]) / self.dc - (vort[self.v2] - vort[self.v1]) / self.dv)
         return tend_h, tend_u
 
-    def tracer_tendency(self, h, u, tr, dt):
+    def tracer_tendency(self, h, u, tr, dt, hE=None, ocean=False):
         """Tracer mass tendency [nC][L][T] of a stage state (FCT of apps/ocean/tasks/
-        solve.cc:99-326 on the sw thickness flux, plus del2 mixing of :328-366)."""
+        solve.cc:99-326 on the thickness flux, plus del2 mixing of :328-366).  sw: the
+        edge thickness is the cells' mean and, without FCT, the centred flux advects;
+        ocean (apps/ocean/run.cc:20-42): the given layerThicknessEdge hE, and
+        without FCT nothing advects."""
         c1, c2 = self.c1, self.c2
-        he = 0.5 * (h[c1] + h[c2])
+        he = 0.5 * (h[c1] + h[c2]) if hE is None else hE
         ntf = (u * he)[:, :, None]                                     # normal thickness flux
         dv = self.dv[:, :, None]
         ce, ee = self.c2e_c, self.c2e_e
@@ -167,10 +170,12 @@ class SwComplex:
             hol = _smax(0.0, ho) * _smin(rm[c1], rp[c2]) + _smin(0.0, ho) * _smin(rp[c1], rm[c2])
             np.add.at(tend_lo, ce, sgn_area * hol[ee])
             tend = tend_lo
-        else:  # centred flux (apps/sw/tasks/solve.cc:237-270)
+        elif not ocean:  # centred flux (apps/sw/tasks/solve.cc:237-270)
             flux = dv * ntf * (0.5 * (tr[c1] + tr[c2]))
             tend = self._scatter3(c2, flux / self.area[c2][:, :, None]) - \
                 self._scatter3(c1, flux / self.area[c1][:, :, None])
+        else:
+            tend = np.zeros(tr.shape, np.result_type(tr, u, he))
         if self.hmix:
             rho = self.msd * self.kappa * dv / self.dc[:, :, None]
             fl = he[:, :, None] * (tr[c2] - tr[c1]) * rho
@@ -219,6 +224,33 @@ class SwComplex:
               + 1j * eps * np.asarray(vt).reshape(self.nC, self.L, self.T))
         hN, uN, tN = self.step(hc, uc, dt, nsteps, tr=tc)
         return hN.imag / eps, uN.imag / eps, tN.imag / eps
+
+    def ocean_step(self, h, hE, u, tr, dt, nsteps=1):
+        """nsteps RK4 steps of the ocean app's tracers (apps/ocean/run.cc:10-50): thickness,
+        edge thickness and velocity prescribed; tr_s = tr0 + w_sub T_{s-1}, tr_new =
+        tr0 + sum w T_s (apps/ocean/tasks/solve.cc:368-399, no thickness weighting)."""
+        h = np.asarray(h).reshape(self.nC, self.L)
+        hE = np.asarray(hE).reshape(self.nE, self.L)
+        u = np.asarray(u).reshape(self.nE, self.L)
+        tr = np.asarray(tr).reshape(self.nC, self.L, self.T)
+        w = (dt / 6, dt / 3, dt / 3, dt / 6)
+        sub = (dt / 2, dt / 2, dt)
+        for _ in range(nsteps):
+            tp, tn = tr, tr.copy()
+            for rk in range(4):
+                tq = self.tracer_tendency(h, u, tp, dt, hE=hE, ocean=True)
+                tn = tn + w[rk] * tq
+                if rk < 3:
+                    tp = tr + sub[rk] * tq
+            tr = tn
+        return tr
+
+    def ocean_jvp(self, h, hE, u, tr, vt, dt, nsteps, eps=1e-30):
+        """Directional derivative of the ocean app's final tracers along vt (complex step,
+        limiter branches decided on the real parts)."""
+        tc = (np.asarray(tr, complex).reshape(self.nC, self.L, self.T)
+              + 1j * eps * np.asarray(vt).reshape(self.nC, self.L, self.T))
+        return self.ocean_step(h, hE, u, tc, dt, nsteps).imag / eps
 
     def jvp(self, h, u, vh, vu, dt, nsteps, eps=1e-30):
         """Directional derivative of (h_N, u_N) along (vh, vu) by the complex step."""

@@ -128,6 +128,34 @@ def test_complex_step_restatement_with_tracers(fct, hmix):
     assert np.abs(jv[2].ravel() - fd_tr.ravel()).max() <= 1e-7 * np.abs(jv[2]).max()
 
 
+@pytest.mark.parametrize("fct,hmix", [(True, True), (True, False), (False, True)])
+def test_complex_step_restatement_ocean(fct, hmix):
+    """The ocean app's tracer step in the complex-step restatement (prescribed
+    thickness, edge thickness and velocity; no thickness weighting in the RK
+    sums) reproduces the oracle's ocean run to rounding, and its tangent
+    agrees with central differences of the oracle."""
+    import mpaso
+    from mpaso.initial import ocean_state
+    from sw_complex import SwComplex
+    mesh = mpaso.Mesh.icosa(3)
+    dt, L, T, n, kappa = 600.0, 2, 2, 3, 1e5
+    S = Oracle("restatement")
+    h, hE, u, tr = ocean_state(mesh, 7, L, T, clip=False)
+    tr = 0.7 * tr + 0.3 * tr.max() * np.random.default_rng(7).uniform(0.0, 1.0, tr.shape)
+    f = S.fct_statics(mesh, L)
+    cfg = S.config(L, T, fct=fct, hmix=hmix, kappa=kappa)
+    run = lambda t: S.ocean_run(mesh, S.static(mesh, f), cfg, dt, n, h, hE, u, t)  # noqa: E731
+    ref = run(tr)
+    C = SwComplex(mesh, L, fct=f, centred=not fct, T=T, hmix=hmix, kappa=kappa)
+    got = C.ocean_step(h, hE, u, tr, dt, n)
+    assert np.abs(got.ravel() - ref.ravel()).max() <= 1e-12 * np.abs(ref).max()
+    v = np.random.default_rng(1).standard_normal(tr.shape)
+    jv = C.ocean_jvp(h, hE, u, tr, v, dt, n)
+    eps = 1e-6
+    fd = (run(tr + eps * v) - run(tr - eps * v)) / (2 * eps)
+    assert np.abs(jv.ravel() - fd.ravel()).max() <= 1e-5 * np.abs(jv).max()
+
+
 @pytest.mark.skipif(not __import__("oracle").cstep_available(), reason="reference checkout absent")
 @pytest.mark.parametrize("kind", ["icosa3", "hex"])
 def test_complex_step_restatement_pinned_to_reference_code(kind):
