@@ -571,15 +571,37 @@ def ensemble_arm(args):
     specs += [("icosa", int(l)) for l in rng.choice(levels, args.ens_sphere)] if args.ens_sphere else []
     cells = [s[1] * s[1] if s[0] == "hex" else 10 * 4 ** s[1] + 2 for s in specs]
     mine = shard(cells, world, rank)
+    # set-up: meshes, FCT statics and initial states on a pool of host
+    # threads (the C calls release the GIL).  The one-call GPU setup of every
+    # member's statics is timed beside it: its kernels take milliseconds, but
+    # the reference layout it returns ([nE][16] stencils, 8.7 GB here) makes
+    # the copy back to host memory the larger cost on this many small meshes
+    from concurrent.futures import ThreadPoolExecutor
+
+    from mpaso.setup import fct_statics_many
+    threads = os.cpu_count() or 1
+
+    def make_mesh(s):
+        return mpaso.Mesh.hex(s[1], s[1], 10e3, 1e-4) if s[0] == "hex" else mpaso.Mesh.icosa(s[1])
+
     t0 = time.time()
-    members = [mpaso.Mesh.hex(s[1], s[1], 10e3, 1e-4) if s[0] == "hex" else mpaso.Mesh.icosa(s[1])
-               for s in (specs[i] for i in mine)]
-    mfct = [fct_statics(m, 1) for m in members]
-    states = [sw_state(m, 5000 + i, 1, 1) for i, m in zip(mine, members)]
+    with ThreadPoolExecutor(threads) as pool:
+        members = list(pool.map(make_mesh, [specs[i] for i in mine]))
+        t1 = time.time()
+        mfct = list(pool.map(lambda m: fct_statics(m, 1), members))
+        t2 = time.time()
+        fct_statics_many(members, 1, device=local)
+        t3 = time.time()
+        states = list(pool.map(lambda a: sw_state(a[1], 5000 + a[0], 1, 1), zip(mine, members)))
+    t4 = time.time()
     opts = dict(fct=True, hmix=True, kappa=1e3, nu=1e3)
     dt, K, W = 30.0, min(args.steps, 200), args.warmup  # the ensemble workload is 200 steps
     dm = G.DeviceMesh.ensemble(members, mfct, device=local)
-    log(f"ensemble built in {time.time() - t0:.1f}s: {len(members)} members, {dm.nC} cells on rank {rank}")
+    t5 = time.time()
+    setup = {"host_threads": threads, "meshes_s": t1 - t0, "fct_statics_host_threads_s": t2 - t1,
+             "fct_statics_gpu_one_call_s": t3 - t2, "initial_states_s": t4 - t3, "device_mesh_s": t5 - t4,
+             "total_s": (t2 - t0) + (t5 - t3)}
+    log(f"ensemble built in {setup['total_s']:.1f}s: {len(members)} members, {dm.nC} cells on rank {rank}")
     st = G.State(dm, nlev=1, ntr=1, **opts)
     for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
         st.set(f, np.concatenate([s[k] for s in states]))
@@ -641,6 +663,7 @@ def ensemble_arm(args):
                "one_at_a_time_serial": {"value": n * K / t_serial, "unit": "member-steps/s",
                                         "how": "members advanced strictly in turn (wait after each member)"},
                "speedup_vs_serial": t_serial / t_batch,
+               "setup": setup,
                "gpu_launches": st.launches_per_step() * K}
     for d, s in singles:
         s.close()

@@ -115,6 +115,22 @@ typedef struct {
 
 int mpaso_fct_setup(const mpaso_fct_setup_in *in, mpaso_fct_setup_out *out);
 
+/* The same setup computed on GPU `device` (host arrays in and out; the call
+ * returns when the outputs are written).  No counterpart in the reference,
+ * which runs it on the host at start-up (apps/ocean/initialize.cc:391-400).
+ * One thread per cell fits the second-derivative polynomial and one per edge
+ * assembles the advection stencil; offsets and indices are validated on the
+ * host first.  Integer outputs equal mpaso_fct_setup's exactly; derivTwo and
+ * the advection coefficients agree with it to the last-place differences of
+ * CUDA's acos / asin / sin / cos / atan2 against the C library's.  For meshes
+ * of many cells, or ensembles, where the host setup costs ~10 us per cell. */
+int mpaso_fct_setup_device(const mpaso_fct_setup_in *in, mpaso_fct_setup_out *out, int32_t device);
+
+/* The device setup of n meshes in one call (one allocation, one stream):
+ * ins[i] -> outs[i].  An error names the first failing member. */
+int mpaso_fct_setup_device_many(const mpaso_fct_setup_in *ins, mpaso_fct_setup_out *outs, int32_t n,
+                                int32_t device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 # Per-file extra flags: the per-task kernels keep every multiply and add
 # separately rounded so that they reproduce the reference tasks bit for bit.
-FILE_FLAGS = {"tasks.cu": ["-fmad=false"]}
+FILE_FLAGS = {"tasks.cu": ["-fmad=false"], "fct_setup_dev.cu": ["-fmad=false"]}
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 

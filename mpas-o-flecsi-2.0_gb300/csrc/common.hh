@@ -2,9 +2,14 @@
 // the space-filling-curve keys used to renumber meshes.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
+#include <exception>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "mpaso_mesh.h"
 
@@ -23,6 +28,39 @@ void set_last_error(const std::string &msg);
 
 inline void require(bool ok, int code, const std::string &msg) {
   if (!ok) fail(code, msg);
+}
+// The message is only turned into a std::string on failure: checks inside
+// per-element loops cost a compare, not an allocation.
+inline void require(bool ok, int code, const char *msg) {
+  if (!ok) fail(code, msg);
+}
+
+// f(i) for i in [0, n) on the host's threads, in contiguous ranges of at
+// least `grain` iterations (one thread when n is small).  For loops whose
+// iterations write disjoint outputs; an exception in any range is rethrown
+// on the calling thread after every range has finished.
+template <class F> void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14) {
+  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+  const int64_t nt = std::min<int64_t>(hw, (n + grain - 1) / std::max<int64_t>(grain, 1));
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::exception_ptr ep;
+  std::mutex mu;
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int64_t t = 0; t < nt; ++t)
+    th.emplace_back([&, t] {
+      try {
+        for (int64_t i = n * t / nt, e = n * (t + 1) / nt; i < e; ++i) f(i);
+      } catch (...) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!ep) ep = std::current_exception();
+      }
+    });
+  for (auto &x : th) x.join();
+  if (ep) std::rethrow_exception(ep);
 }
 
 // Runs `body` and maps exceptions to MPASO_ERR_* codes + the thread-local message.

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <numeric>
 
 #include "device.cuh"
@@ -51,10 +52,10 @@ Crs copy_crs(const int64_t *off, const int32_t *idx, int64_t n, int64_t n_to, co
   c.off.assign(off, off + n + 1);
   require(c.off[0] == 0, MPASO_ERR_MESH, std::string(name) + ": offsets must start at 0");
   for (int64_t i = 0; i < n; ++i)
-    require(c.off[i + 1] >= c.off[i], MPASO_ERR_MESH, std::string(name) + ": offsets decrease");
+    if (c.off[i + 1] < c.off[i]) fail(MPASO_ERR_MESH, std::string(name) + ": offsets decrease");
   c.idx.assign(idx, idx + c.off[n]);
   for (int32_t v : c.idx)
-    require(v >= 0 && v < n_to, MPASO_ERR_MESH, std::string(name) + ": index out of range");
+    if (v < 0 || v >= n_to) fail(MPASO_ERR_MESH, std::string(name) + ": index out of range");
   return c;
 }
 
@@ -71,7 +72,9 @@ Crs transpose(const Crs &a, int64_t n_to) {
   return t;
 }
 
-// Device arena: sub-allocations aligned to 256 B inside one cudaMalloc.
+// Device arena: sub-allocations aligned to 256 B inside one cudaMalloc.  It
+// keeps pointers to the host vectors, which must stay alive until upload();
+// each is copied once, straight into its slice.
 struct Arena {
   struct Item {
     const void *src;
@@ -80,11 +83,9 @@ struct Arena {
     const void **dst;
   };
   std::vector<Item> items;
-  std::vector<std::vector<char>> owned;
   size_t total = 0;
   template <class T> void add(const std::vector<T> &v, const T **dst) {
-    owned.emplace_back((const char *)v.data(), (const char *)v.data() + v.size() * sizeof(T));
-    items.push_back({owned.back().data(), v.size() * sizeof(T), total, (const void **)dst});
+    items.push_back({v.data(), v.size() * sizeof(T), total, (const void **)dst});
     total += (v.size() * sizeof(T) + 255) & ~size_t(255);
   }
   void upload(MeshCtx &ctx) {
@@ -93,9 +94,8 @@ struct Arena {
       fail(MPASO_ERR_ALLOC, "device allocation of the mesh context failed");
     }
     ctx.arena_bytes = total;
-    std::vector<char> host(total, 0);
-    for (auto &it : items) std::memcpy(host.data() + it.off, it.src, it.bytes);
-    MPASO_CUDA(cudaMemcpy(ctx.arena, host.data(), total, cudaMemcpyHostToDevice));
+    for (auto &it : items)
+      if (it.bytes) MPASO_CUDA(cudaMemcpy((char *)ctx.arena + it.off, it.src, it.bytes, cudaMemcpyHostToDevice));
     for (auto &it : items) *it.dst = (const char *)ctx.arena + it.off;
   }
 };
@@ -167,7 +167,8 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     const std::vector<int64_t> whole = {0, nC};
     const std::vector<int64_t> &blk = mcells ? *mcells : whole;
     std::vector<uint64_t> key(nC);
-    for (size_t b = 0; b + 1 < blk.size(); ++b) {
+    boxes.resize(blk.size() - 1);
+    parallel_for((int64_t)blk.size() - 1, [&](int64_t b) {
       const int64_t c0 = blk[b], c1 = blk[b + 1];
       Box B{{1e300, 1e300, 1e300}, {-1e300, -1e300, -1e300}, 2, 30};
       for (int a = 0; a < 3; ++a)
@@ -176,7 +177,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
       // a member whose z is absent or constant (a plane) is ordered in 2-D
       B.dims = (d.zCell && B.hi[2] > B.lo[2]) ? 3 : 2;
       B.bits = B.dims == 3 ? 20 : 30;
-      boxes.push_back(B);
+      boxes[b] = B;
       for (int64_t c = c0; c < c1; ++c) {
         double p[3];
         uint32_t q[3];
@@ -185,10 +186,19 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
         key[c] = d.reorder == 3 ? morton_key(q, B.dims, B.bits) : hilbert_key(q, B.dims, B.bits);
         member[c] = (int32_t)b;
       }
-    }
-    std::stable_sort(pc.begin(), pc.end(), [&](int32_t a, int32_t b) {
-      return member[a] != member[b] ? member[a] < member[b] : key[a] < key[b];
+    }, 1);
+    // (member, key, id) tuples sorted once: the unique id as the last key
+    // gives the order a stable sort by (member, key) gives
+    struct CK {
+      int32_t m, id;
+      uint64_t k;
+    };
+    std::vector<CK> ck(nC);
+    parallel_for(nC, [&](int64_t c) { ck[c] = CK{member[c], (int32_t)c, key[c]}; });
+    std::sort(ck.begin(), ck.end(), [](const CK &a, const CK &b) {
+      return a.m != b.m ? a.m < b.m : a.k != b.k ? a.k < b.k : a.id < b.id;
     });
+    for (int64_t k = 0; k < nC; ++k) pc[k] = ck[k].id;
   }
   std::vector<int32_t> ic(nC);
   for (int64_t k = 0; k < nC; ++k) ic[pc[k]] = (int32_t)k;
@@ -217,17 +227,23 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     std::stable_sort(pe.begin(), pe.end(), [&](int32_t a, int32_t b) { return ek[a] < ek[b]; });
     std::stable_sort(pv.begin(), pv.end(), [&](int32_t a, int32_t b) { return vk[a] < vk[b]; });
   } else if (d.reorder) {
-    auto ekey = [&](int32_t e) {
-      const int32_t a = ic[e2c.at(e, 0)], b = ic[e2c.at(e, 1)];
-      return std::make_pair(std::min(a, b), std::max(a, b));
-    };
-    std::stable_sort(pe.begin(), pe.end(), [&](int32_t a, int32_t b) { return ekey(a) < ekey(b); });
-    auto vkey = [&](int32_t v) {
+    // edges by (lower, higher) new id of their cells, vertices by the lowest
+    // new id of theirs; keys computed once, ties by the old id (= a stable sort)
+    std::vector<std::pair<uint64_t, int32_t>> ek(nE);
+    parallel_for(nE, [&](int64_t e) {
+      const uint32_t a = (uint32_t)ic[e2c.at(e, 0)], b = (uint32_t)ic[e2c.at(e, 1)];
+      ek[e] = {((uint64_t)std::min(a, b) << 32) | std::max(a, b), (int32_t)e};
+    });
+    std::sort(ek.begin(), ek.end());
+    for (int64_t k = 0; k < nE; ++k) pe[k] = ek[k].second;
+    std::vector<std::pair<uint64_t, int32_t>> vk(nV);
+    parallel_for(nV, [&](int64_t v) {
       int32_t m = INT32_MAX;
       for (int j = 0; j < kVertexDegree; ++j) m = std::min(m, ic[v2c.at(v, j)]);
-      return m;
-    };
-    std::stable_sort(pv.begin(), pv.end(), [&](int32_t a, int32_t b) { return vkey(a) < vkey(b); });
+      vk[v] = {(uint64_t)(uint32_t)m, (int32_t)v};
+    });
+    std::sort(vk.begin(), vk.end());
+    for (int64_t k = 0; k < nV; ++k) pv[k] = vk[k].second;
   }
   std::vector<int32_t> ie(nE), iv(nV);
   for (int64_t k = 0; k < nE; ++k) ie[pe[k]] = (int32_t)k;
@@ -243,7 +259,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   std::vector<double> area(nC), invArea(nC), hs(nC, 0.0);
   std::vector<int> mlc(nC, 1);
   const Crs c2eAsc = transpose(e2c, nC);  // edges of each cell, ascending reference id
-  for (int64_t k = 0; k < nC; ++k) {
+  parallel_for(nC, [&](int64_t k) {
     const int32_t c = pc[k];
     const int n = (int)c2e.len(c);
     nEoC[k] = n;
@@ -271,7 +287,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     invArea[k] = 1.0 / d.areaCell[c];
     if (d.bottomDepth) hs[k] = d.bottomDepth[c];
     if (d.maxLevelCell) mlc[k] = d.maxLevelCell[c];
-  }
+  });
   A.add(nEoC, &m.nEoC), A.add(eoc, &m.eoc), A.add(eocSign, &m.eocSign), A.add(eocAsc, &m.eocAsc);
   A.add(eocAscSign, &m.eocAscSign), A.add(coc, &m.coc), A.add(nbr, &m.nbr), A.add(area, &m.areaCell);
   A.add(invArea, &m.invAreaCell), A.add(hs, &m.bottomDepth), A.add(mlc, &m.maxLevelCell);
@@ -281,7 +297,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   std::vector<double> dv(nE), dc(nE), idc(nE), idv(nE), msd(nE, 1.0);
   std::vector<int> nEoE(nE), eoe((size_t)std::max(maxEoE, 1) * nE), mlet(nE, 1);
   std::vector<double> woe((size_t)std::max(maxEoE, 1) * nE, 0.0);
-  for (int64_t k = 0; k < nE; ++k) {
+  parallel_for(nE, [&](int64_t k) {
     const int32_t e = pe[k];
     coe[k] = make_int2(ic[e2c.at(e, 0)], ic[e2c.at(e, 1)]);
     voe[k] = make_int2(iv[e2v.at(e, 0)], iv[e2v.at(e, 1)]);
@@ -300,7 +316,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     }
     if (d.maxLevelEdgeTop) mlet[k] = d.maxLevelEdgeTop[e];
     if (d.meshScalingDel2) msd[k] = d.meshScalingDel2[e];
-  }
+  });
   A.add(coe, &m.coe), A.add(voe, &m.voe), A.add(dv, &m.dvEdge), A.add(dc, &m.dcEdge);
   A.add(idc, &m.invDcEdge), A.add(idv, &m.invDvEdge), A.add(nEoE, &m.nEoE), A.add(eoe, &m.eoe);
   A.add(woe, &m.woe), A.add(mlet, &m.maxLevelEdgeTop), A.add(msd, &m.meshScalingDel2);
@@ -321,7 +337,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   std::vector<double> ac((size_t)maxAdv * nE, 0.0), a3((size_t)maxAdv * nE, 0.0);
   std::vector<double> cp((size_t)maxAdv * nE, 0.0), cm((size_t)maxAdv * nE, 0.0);
   if (ctx.has_fct) {
-    for (int64_t k = 0; k < nE; ++k) {
+    parallel_for(nE, [&](int64_t k) {
       const int32_t e = pe[k];
       const int n = d.nAdvCellsForEdge[e];
       nAdv[k] = n;
@@ -340,7 +356,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
         }
       }
       for (int l = 0; l < m.fctLev; ++l) mask[(size_t)k * m.fctLev + l] = d.highOrderAdvMask[(size_t)e * m.fctLev + l];
-    }
+    });
   }
   A.add(nAdv, &m.nAdv), A.add(advCells, &m.advCells), A.add(ac, &m.advCoef), A.add(a3, &m.advCoef3);
   A.add(cp, &m.advCp), A.add(cm, &m.advCm), A.add(mask, &m.hoMask);
@@ -349,7 +365,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   std::vector<int> cov((size_t)kVertexDegree * nV), eov((size_t)kVertexDegree * nV);
   std::vector<double> kite((size_t)kVertexDegree * nV), eovSign((size_t)kVertexDegree * nV);
   std::vector<double> aT(nV), iaT(nV), fV(nV);
-  for (int64_t k = 0; k < nV; ++k) {
+  parallel_for(nV, [&](int64_t k) {
     const int32_t v = pv[k];
     for (int j = 0; j < kVertexDegree; ++j) {
       const size_t s = (size_t)j * nV + k;
@@ -360,7 +376,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
       eovSign[s] = (e2v.at(e, 0) == v) ? -1.0 : 1.0;
     }
     aT[k] = d.areaTriangle[v], iaT[k] = 1.0 / d.areaTriangle[v], fV[k] = d.fVertex[v];
-  }
+  });
   A.add(cov, &m.cov), A.add(kite, &m.kite), A.add(eov, &m.eov), A.add(eovSign, &m.eovSign);
   A.add(aT, &m.areaTriangle), A.add(iaT, &m.invAreaTriangle), A.add(fV, &m.fVertex);
 
@@ -368,7 +384,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   // e' in edgesOnEdge(e) <=> e in edgesOnEdge(e') (both share a cell), so the
   // transposed stencil of e is its own stencil with the partner's weight.
   std::vector<double> woeT((size_t)std::max(maxEoE, 1) * nE, 0.0);
-  for (int64_t k = 0; k < nE; ++k)
+  parallel_for(nE, [&](int64_t k) {
     for (int j = 0; j < nEoE[k]; ++j) {
       const int eo = eoe[(size_t)j * nE + k];
       int p = 0;
@@ -376,6 +392,7 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
       require(p < nEoE[eo], MPASO_ERR_MESH, "edgesOnEdge is not symmetric");
       woeT[(size_t)j * nE + k] = woe[(size_t)p * nE + eo];
     }
+  });
   std::vector<int> vocR((size_t)maxEoC * nC, 0);
   std::vector<double> kiteR((size_t)maxEoC * nC, 0.0);
   std::vector<int> fillc(nC, 0);
@@ -393,30 +410,61 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
   // cell -> entries of the advection stencils that read the cell: the edge
   // (ascending; -1 pads at the end of each column) and the coefficient pair
   // {advCoef + 0.25 advCoef_3rd, advCoef - 0.25 advCoef_3rd} of the cell there
-  std::vector<std::vector<int>> rev(ctx.has_fct ? nC : 0);
-  for (int64_t k = 0; ctx.has_fct && k < nE; ++k)
-    for (int j = 0; j < nAdv[k]; ++j) rev[advCells[(size_t)j * nE + k]].push_back((int)(j * nE + k));
+  // (counted CSR, filled in ascending edge order).  Ensemble members own
+  // disjoint blocks of cells and of edges, so members fill in parallel; the
+  // edge blocks are found from the members of the edges' cells, which do not
+  // decrease along the edge numbering (one block when they would).
+  std::vector<int64_t> eblk = {0, nE};
+  if (mcells && mcells->size() > 2) {
+    const std::vector<int64_t> &mc = *mcells;
+    auto member_of = [&](int64_t k) {
+      return std::upper_bound(mc.begin(), mc.end(), (int64_t)coe[k].x) - mc.begin() - 1;
+    };
+    std::vector<int64_t> b = {0};
+    bool mono = true;
+    for (int64_t k = 1; k < nE && mono; ++k) {
+      const auto a = member_of(k - 1), c = member_of(k);
+      if (c < a) mono = false;
+      if (c != a) b.push_back(k);
+    }
+    b.push_back(nE);
+    if (mono) eblk = b;
+  }
+  const int64_t nblk = (int64_t)eblk.size() - 1;
+  std::vector<int> revN(ctx.has_fct ? nC : 0, 0);
+  if (ctx.has_fct)
+    parallel_for(nblk, [&](int64_t b) {
+      for (int64_t k = eblk[b]; k < eblk[b + 1]; ++k)
+        for (int j = 0; j < nAdv[k]; ++j) revN[advCells[(size_t)j * nE + k]]++;
+    }, 1);
   int maxAdvR = 1;
-  for (auto &r : rev) maxAdvR = std::max(maxAdvR, (int)r.size());
+  for (int r : revN) maxAdvR = std::max(maxAdvR, r);
   std::vector<int> advRe((size_t)maxAdvR * nC, -1);
   std::vector<double> advRc((size_t)2 * maxAdvR * nC, 0.0);
-  for (size_t c = 0; c < rev.size(); ++c)
-    for (size_t j = 0; j < rev[c].size(); ++j) {
-      const size_t sa = (size_t)rev[c][j], o = j * nC + c;
-      advRe[o] = (int)(sa % (size_t)nE);
-      advRc[2 * o] = cp[sa], advRc[2 * o + 1] = cm[sa];
-    }
+  std::fill(revN.begin(), revN.end(), 0);
+  if (ctx.has_fct)
+    parallel_for(nblk, [&](int64_t b) {
+      for (int64_t k = eblk[b]; k < eblk[b + 1]; ++k)
+        for (int j = 0; j < nAdv[k]; ++j) {
+          const size_t sa = (size_t)j * nE + k;
+          const int c = advCells[sa];
+          const size_t o = (size_t)revN[c]++ * nC + c;
+          advRe[o] = (int)k;
+          advRc[2 * o] = cp[sa], advRc[2 * o + 1] = cm[sa];
+        }
+    }, 1);
   m.maxAdvR = maxAdvR;
   A.add(advRe, &m.advRe), A.add(advRc, (const double **)&m.advRc);
   // cellsOnCell with the cell itself and repeated neighbours replaced by -1
   std::vector<int> cocU((size_t)maxEoC * nC, -1);
-  for (int64_t c = 0; c < nC; ++c)
+  parallel_for(nC, [&](int64_t c) {
     for (int j = 0; j < nEoC[c]; ++j) {
       const int o = coc[(size_t)j * nC + c];
       bool dup = o == (int)c;
       for (int p = 0; p < j && !dup; ++p) dup = coc[(size_t)p * nC + c] == o;
       if (!dup) cocU[(size_t)j * nC + c] = o;
     }
+  });
   A.add(cocU, &m.cocU);
 
   A.upload(ctx);
@@ -434,10 +482,19 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
 // first cell / edge / vertex.  The vectors in `keep` own the arrays `u`
 // points at.
 struct Union {
+  // uninitialised host buffers: their pages are first touched by the
+  // parallel member copies, not by a zero fill on one thread
+  template <class T> struct Buf {
+    std::unique_ptr<T[]> p;
+    T *alloc(size_t n) {
+      p.reset(new T[std::max<size_t>(n, 1)]);
+      return p.get();
+    }
+  };
   mpaso_mesh_desc u{};
-  std::vector<std::vector<int64_t>> offs;
-  std::vector<std::vector<int32_t>> ints;
-  std::vector<std::vector<double>> dbls;
+  std::vector<Buf<int64_t>> offs;
+  std::vector<Buf<int32_t>> ints;
+  std::vector<Buf<double>> dbls;
   std::vector<int64_t> mcells, medges, mverts;
 };
 
@@ -468,47 +525,56 @@ void make_union(Union &U, const mpaso_mesh_desc *m, int n) {
                    {&mpaso_mesh_desc::c2c_off, &mpaso_mesh_desc::c2c, &U.mcells, &U.mcells},
                    {&mpaso_mesh_desc::e2v_off, &mpaso_mesh_desc::e2v, &U.medges, &U.mverts},
                    {&mpaso_mesh_desc::e2e_off, &mpaso_mesh_desc::e2e, &U.medges, &U.medges}};
+  // every union array is sized once and each member copies into its own
+  // slice, members in parallel
   for (const C &c : cs) {
-    std::vector<int64_t> off = {0};
-    std::vector<int32_t> idx;
+    std::vector<int64_t> ibase(n + 1, 0);
     for (int i = 0; i < n; ++i) {
       const int64_t *o = m[i].*c.off;
-      const int32_t *x = m[i].*c.idx;
-      require(o && x, MPASO_ERR_ARG, "member connectivity missing");
-      const int64_t rows = (*c.rows)[i + 1] - (*c.rows)[i], shift = (*c.to)[i];
-      const int64_t base = off.back();
-      for (int64_t r = 0; r < rows; ++r) off.push_back(base + o[r + 1]);
-      for (int64_t k = 0; k < o[rows]; ++k) idx.push_back((int32_t)(x[k] + shift));
+      require(o && m[i].*c.idx, MPASO_ERR_ARG, "member connectivity missing");
+      ibase[i + 1] = ibase[i] + o[(*c.rows)[i + 1] - (*c.rows)[i]];
     }
-    U.offs.push_back(std::move(off));
-    U.ints.push_back(std::move(idx));
-    u.*c.off = U.offs.back().data();
-    u.*c.idx = U.ints.back().data();
+    U.offs.emplace_back();
+    U.ints.emplace_back();
+    int64_t *off = U.offs.back().alloc((size_t)c.rows->back() + 1);
+    int32_t *idx = U.ints.back().alloc((size_t)ibase[n]);
+    off[0] = 0;
+    parallel_for(n, [&](int64_t i) {
+      const int64_t *o = m[i].*c.off;
+      const int32_t *x = m[i].*c.idx;
+      const int64_t r0 = (*c.rows)[i], rows = (*c.rows)[i + 1] - r0, shift = (*c.to)[i], base = ibase[i];
+      for (int64_t r = 0; r < rows; ++r) off[r0 + r + 1] = base + o[r + 1];
+      for (int64_t k = 0; k < o[rows]; ++k) idx[base + k] = (int32_t)(x[k] + shift);
+    }, 1);
+    u.*c.off = off;
+    u.*c.idx = idx;
   }
   // per-entity fields: (member, values per entity, entity rows, default when NULL)
   auto cat = [&](const double *mpaso_mesh_desc::*f, int per, const std::vector<int64_t> &rows,
                  bool may_be_null) -> const double * {
-    std::vector<double> v;
-    v.reserve((size_t)rows.back() * per);
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i) require(m[i].*f || may_be_null, MPASO_ERR_ARG, "member geometry field missing");
+    U.dbls.emplace_back();
+    double *v = U.dbls.back().alloc((size_t)rows.back() * per);
+    parallel_for(n, [&](int64_t i) {
       const double *x = m[i].*f;
+      double *y = v + rows[i] * per;
       const int64_t cnt = (rows[i + 1] - rows[i]) * per;
-      require(x || may_be_null, MPASO_ERR_ARG, "member geometry field missing");
-      for (int64_t k = 0; k < cnt; ++k) v.push_back(x ? x[k] : 0.0);
-    }
-    U.dbls.push_back(std::move(v));
-    return U.dbls.back().data();
+      if (x)
+        std::copy(x, x + cnt, y);
+      else
+        std::fill(y, y + cnt, 0.0);
+    }, 1);
+    return v;
   };
   auto cati = [&](const int32_t *mpaso_mesh_desc::*f, int per, const std::vector<int64_t> &rows) -> const int32_t * {
-    std::vector<int32_t> v;
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i) require(m[i].*f, MPASO_ERR_ARG, "member FCT field missing");
+    U.ints.emplace_back();
+    int32_t *v = U.ints.back().alloc((size_t)rows.back() * per);
+    parallel_for(n, [&](int64_t i) {
       const int32_t *x = m[i].*f;
-      require(x, MPASO_ERR_ARG, "member FCT field missing");
-      const int64_t cnt = (rows[i + 1] - rows[i]) * per;
-      for (int64_t k = 0; k < cnt; ++k) v.push_back(x[k]);
-    }
-    U.ints.push_back(std::move(v));
-    return U.ints.back().data();
+      std::copy(x, x + (rows[i + 1] - rows[i]) * per, v + rows[i] * per);
+    }, 1);
+    return v;
   };
   u.areaCell = cat(&mpaso_mesh_desc::areaCell, 1, U.mcells, false);
   u.dvEdge = cat(&mpaso_mesh_desc::dvEdge, 1, U.medges, false);
@@ -532,18 +598,19 @@ void make_union(Union &U, const mpaso_mesh_desc *m, int n) {
     u.nAdvCellsForEdge = cati(&mpaso_mesh_desc::nAdvCellsForEdge, 1, U.medges);
     u.highOrderAdvMask = cati(&mpaso_mesh_desc::highOrderAdvMask, L, U.medges);
     // advection cells: the first nAdv entries of each row shift by the member's first cell
-    std::vector<int32_t> adv;
-    adv.reserve((size_t)u.nEdges * kMaxEdges2);
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n; ++i)
       require(m[i].advCellsForEdge && m[i].nAdvCellsForEdge, MPASO_ERR_ARG, "member FCT field missing");
+    U.ints.emplace_back();
+    int32_t *adv = U.ints.back().alloc((size_t)u.nEdges * kMaxEdges2);
+    parallel_for(n, [&](int64_t i) {
+      int32_t *y = adv + U.medges[i] * kMaxEdges2;
       for (int64_t e = 0; e < m[i].nEdges; ++e)
         for (int j = 0; j < kMaxEdges2; ++j) {
           const int32_t x = m[i].advCellsForEdge[e * kMaxEdges2 + j];
-          adv.push_back(j < m[i].nAdvCellsForEdge[e] ? (int32_t)(x + U.mcells[i]) : x);
+          y[e * kMaxEdges2 + j] = j < m[i].nAdvCellsForEdge[e] ? (int32_t)(x + U.mcells[i]) : x;
         }
-    }
-    U.ints.push_back(std::move(adv));
-    u.advCellsForEdge = U.ints.back().data();
+    }, 1);
+    u.advCellsForEdge = adv;
     u.edgeSignOnCell = cat(&mpaso_mesh_desc::edgeSignOnCell, kMaxEdges, U.mcells, false);
     u.advCoef = cat(&mpaso_mesh_desc::advCoef, kMaxEdges2, U.medges, false);
     u.advCoef_3rd = cat(&mpaso_mesh_desc::advCoef_3rd, kMaxEdges2, U.medges, false);

@@ -105,8 +105,22 @@ class Mesh:
         return Mesh(h), (pc, pe, pv)
 
     # ---- reference read semantics ----
+    _CRS_SOURCES = ("verticesOnCell", "edgesOnCell", "cellsOnCell", "verticesOnEdge", "edgesOnEdge")
+
     def crs(self):
-        """Connectivity as the reference's mesh holds it: dict name -> (offsets, indices)."""
+        """Connectivity as the reference's mesh holds it: dict name -> (offsets, indices).
+        Built once and kept while the five file connectivity arrays are the same
+        objects (the result is shared: treat it as read-only)."""
+        f = self.fields
+        src = tuple(f.get(n) for n in self._CRS_SOURCES)
+        cached = getattr(self, "_crs_cache", None)
+        if cached is not None and all(a is b for a, b in zip(cached[0], src)):
+            return cached[1]
+        out = self._build_crs()
+        self._crs_cache = (src, out)
+        return out
+
+    def _build_crs(self):
         f = self.fields
 
         def from_file(name):

@@ -1,8 +1,11 @@
-"""Host-side FCT / del2 static coefficients (libmpaso's mpaso_fct_setup).
+"""FCT / del2 static coefficients (libmpaso's mpaso_fct_setup, or
+mpaso_fct_setup_device on a GPU).
 
 The setup of apps/ocean/tasks/init_functions.cc:18-447, bit-identical to the
-reference on the sphere; on a periodic plane it fits the same polynomial in
-plane coordinates (the reference leaves that branch empty)."""
+reference on the sphere when run on the host; on a periodic plane it fits the
+same polynomial in plane coordinates (the reference leaves that branch
+empty).  On the GPU the integer outputs are identical and the coefficients
+agree to the last-place differences of CUDA's trigonometric functions."""
 import ctypes
 
 import numpy as np
@@ -30,8 +33,27 @@ class _Out(ctypes.Structure):
                 ("highOrderAdvMask", _ip), ("advCoef", _dp), ("advCoef_3rd", _dp)]
 
 
-def fct_statics(mesh, nlev, maxLevelCell=None, boundaryCell=None):
-    """Returns the FCT statics as a dict of numpy arrays (reference layouts)."""
+def fct_statics(mesh, nlev, maxLevelCell=None, boundaryCell=None, device=None):
+    """Returns the FCT statics as a dict of numpy arrays (reference layouts);
+    device = a CUDA device index computes them on that GPU."""
+    i, o, out, keep = _setup_args(mesh, nlev, maxLevelCell, boundaryCell)
+    if device is None:
+        check(lib().mpaso_fct_setup(ctypes.byref(i), ctypes.byref(o)))
+    else:
+        check(lib().mpaso_fct_setup_device(ctypes.byref(i), ctypes.byref(o), ctypes.c_int32(int(device))))
+    return out
+
+
+def fct_statics_many(meshes, nlev, device=0):
+    """FCT statics of every mesh in one device call (mpaso_fct_setup_device_many)."""
+    args = [_setup_args(m, nlev, None, None) for m in meshes]
+    ins = (_In * len(args))(*[a[0] for a in args])
+    outs = (_Out * len(args))(*[a[1] for a in args])
+    check(lib().mpaso_fct_setup_device_many(ins, outs, ctypes.c_int32(len(args)), ctypes.c_int32(int(device))))
+    return [a[2] for a in args]
+
+
+def _setup_args(mesh, nlev, maxLevelCell, boundaryCell):
     crs = mesh.crs()
     f = mesh.fields
     nC, nE = mesh.nCells, mesh.nEdges
@@ -65,6 +87,5 @@ def fct_statics(mesh, nlev, maxLevelCell=None, boundaryCell=None):
         "advCoef_3rd": np.zeros((nE, 16)),
     }
     o = _Out(**{k: v.ctypes.data_as(_dp if v.dtype == np.float64 else _ip) for k, v in out.items()})
-    check(lib().mpaso_fct_setup(ctypes.byref(i), ctypes.byref(o)))
     out["maxLevelCell"] = mlc
-    return out
+    return i, o, out, keep
