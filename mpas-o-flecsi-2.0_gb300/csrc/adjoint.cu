@@ -728,7 +728,13 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
         launch_pdl(k_adj_tr_a<NLA, 0>, nC * NLA, TPB, pdl, st, m, t, L);
     }
     launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
-    launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
+    // two lanes per cell-level hide gather latency on small meshes; with a
+    // million cell-levels or more there is parallelism enough, and the
+    // second lane only idles through the per-cell tail on the FP64 pipe
+    if (nC >= (1 << 20))
+      launch_pdl(k_adj_tr_c<1>, nC, TPB, pdl, st, m, t, L);
+    else
+      launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
     a.lFt = A.lFt, a.lhet = A.lhet, a.muh_t = A.muh_t;
   }
   if (ocean) return;  // the ocean's h and u are prescribed: nothing more to reverse

@@ -78,6 +78,28 @@ def test_ocean_adjoint_sixty_levels(level):
     assert abs(lhs - rhs) <= 1e-10 * np.abs(w * jv).sum(), (lhs, rhs)
 
 
+def test_ocean_adjoint_one_lane_per_cell_level():
+    """At a million cell-levels and more the tracer gather runs one thread per
+    cell-level instead of two: 1700 levels on a level-3 sphere (1.09M
+    cell-levels) hold that path to the same 1e-10 dot-product bar."""
+    import mpaso.gpu as G
+    from sw_complex import SwComplex
+    L, T, dt, n = 1700, 1, 450.0, 2
+    mesh, f, st, (h, hE, u, tr) = make(L, T, dict(fct=True, hmix=True, kappa=1e4), level=3, seed=1234,
+                                       noise=False)
+    assert mesh.nCells * L >= 1 << 20
+    rng = np.random.default_rng(4)
+    w = rng.standard_normal(tr.shape)
+    st.set(G.FIELD_TRACERS, tr)
+    st.forward(dt, n, 1)
+    gt = st.vjp_tracers(np.zeros(h.shape), np.zeros(u.shape), w)[2]
+    C = SwComplex(mesh, L, fct=f, T=T, hmix=True, kappa=1e4)
+    v = rng.standard_normal(tr.shape)
+    jv = C.ocean_jvp(h, hE, u, tr, v, dt, n)
+    lhs, rhs = float((w * jv).sum()), float((gt * v).sum())
+    assert abs(lhs - rhs) <= 1e-10 * np.abs(w * jv).sum(), (lhs, rhs)
+
+
 def test_ocean_adjoint_fd_checkpoints_and_stored_window():
     import mpaso.gpu as G
     L, T, dt, n = 1, 3, 600.0, 5
