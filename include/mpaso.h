@@ -226,6 +226,13 @@ int mpaso_state_destroy(mpaso_state s);
 int mpaso_state_set(mpaso_state s, int32_t field, const double *data);
 /* Copy a field out (reference numbering, host or device memory). */
 int mpaso_state_get(mpaso_state s, int32_t field, double *data);
+/* Scan the prognostic fields (h, u, tracers; the ocean's edge thickness) on
+ * the device for NaN or infinity: MPASO_OK, or MPASO_ERR_NUMERIC with the
+ * first offending field, entity (reference numbering), level and tracer in
+ * mpaso_last_error().  No counterpart in the reference, which has no such
+ * check; a blow-up there shows as NaN in the error norms of
+ * apps/sw/finalize.cc:21-23. */
+int mpaso_state_check_finite(mpaso_state s);
 /* Advance nsteps RK4 steps of size dt; asynchronous on the state's stream. */
 int mpaso_rk4_step(mpaso_state s, double dt, int32_t nsteps);
 /* Same, replayed from a CUDA graph of one step (captured on first use for dt). */

@@ -32,8 +32,8 @@ extern "C" {
 #define MPASO_ERR_CUDA 3      /* CUDA runtime error */
 #define MPASO_ERR_ALLOC 4     /* allocation failure (host or device) */
 #define MPASO_ERR_NOTFOUND 5  /* unknown dataset name */
-#define MPASO_ERR_TIMEOUT 6   /* a bounded device-side wait gave up */
-#define MPASO_ERR_NUMERIC 7   /* non-finite value detected where checked */
+#define MPASO_ERR_TIMEOUT 6   /* reserved: a bounded device-side wait gave up (no kernel waits today) */
+#define MPASO_ERR_NUMERIC 7   /* non-finite value found (mpaso_state_check_finite) */
 #define MPASO_ERR_NODEVICE 8  /* no CUDA device available */
 #define MPASO_ERR_IO 9        /* file open / read / write failure or malformed file */
 

@@ -310,6 +310,14 @@ __global__ void k_build_stat(DMesh m, double kappa, double nu, StatOut o) {
   if (i < (int64_t)kVertexDegree * m.nV) o.sdc[i] = m.eovSign[i] * m.dcEdge[m.eov[i]];
 }
 
+// Smallest index of a NaN or infinity in x[0, n) (exponent bits all set;
+// integer pipe only), or first left as it was.
+__global__ void k_first_nonfinite(const double *x, int64_t n, unsigned long long *first) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if ((__double_as_longlong(x[i]) & 0x7ff0000000000000LL) == 0x7ff0000000000000LL)
+      atomicMin(first, (unsigned long long)i);
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ state context
@@ -938,6 +946,49 @@ int mpaso_state_get(mpaso_state s, int32_t field, double *data) {
     k_scatter_rows_pub(buf, dst, ctx.d_perm[entity], n, (int)row, S.stream);
     if (!dev) MPASO_CUDA(cudaMemcpyAsync(data, dst, (size_t)n * row * 8, cudaMemcpyDeviceToHost, S.stream));
     MPASO_CUDA(cudaStreamSynchronize(S.stream));
+  });
+}
+
+int mpaso_state_check_finite(mpaso_state s) {
+  return guarded("mpaso_state_check_finite", [&] {
+    require(s != nullptr, MPASO_ERR_ARG, "null state");
+    SwState &S = s->s;
+    MeshCtx &ctx = S.mesh->ctx;
+    MPASO_CUDA(cudaSetDevice(ctx.device));
+    struct F {
+      int id;
+      const char *name;
+    };
+    std::vector<F> fields = {{MPASO_FIELD_H, "layer thickness"}, {MPASO_FIELD_U, "normal velocity"}};
+    if (S.T > 0) fields.push_back({MPASO_FIELD_TRACERS, "tracer"});
+    if (S.p.app == MPASO_APP_OCEAN) fields.push_back({MPASO_FIELD_LAYER_THICKNESS_EDGE, "edge layer thickness"});
+    auto *first = reinterpret_cast<unsigned long long *>(ensure_io(S, fields.size() * 8));
+    MPASO_CUDA(cudaMemsetAsync(first, 0xff, fields.size() * 8, S.stream));
+    std::vector<int64_t> rows(fields.size());
+    std::vector<int> ents(fields.size());
+    for (size_t f = 0; f < fields.size(); ++f) {
+      double *buf;
+      field_geom(S, fields[f].id, ents[f], rows[f], buf);
+      const int64_t n = (ents[f] == MPASO_CELLS ? ctx.d.nC : ctx.d.nE) * rows[f];
+      k_first_nonfinite<<<152 * 8, 256, 0, S.stream>>>(buf, n, first + f);  // 8 blocks per SM
+    }
+    MPASO_CUDA(cudaGetLastError());
+    std::vector<unsigned long long> h(fields.size());
+    MPASO_CUDA(cudaMemcpyAsync(h.data(), first, fields.size() * 8, cudaMemcpyDeviceToHost, S.stream));
+    MPASO_CUDA(cudaStreamSynchronize(S.stream));
+    for (size_t f = 0; f < fields.size(); ++f) {
+      if (h[f] == ~0ull) continue;
+      // device index -> entity in file order, level (and tracer)
+      const int64_t e = (int64_t)(h[f] / (unsigned long long)rows[f]), comp = (int64_t)(h[f] % rows[f]);
+      const int32_t old = ctx.perm[ents[f]][e];
+      std::string msg = std::string("non-finite ") + fields[f].name + " at " +
+                        (ents[f] == MPASO_CELLS ? "cell " : "edge ") + std::to_string(old) + " level ";
+      if (fields[f].id == MPASO_FIELD_TRACERS)
+        msg += std::to_string(comp / S.T) + " tracer " + std::to_string(comp % S.T);
+      else
+        msg += std::to_string(comp);
+      fail(MPASO_ERR_NUMERIC, msg);
+    }
   });
 }
 

@@ -247,6 +247,11 @@ class State:
                 raise ValueError("field size mismatch")
         check(lib().mpaso_state_set(self._h, int(field), _ptr(data)))
 
+    def check_finite(self):
+        """Raises MpasoError (MPASO_ERR_NUMERIC) naming the first NaN / infinity
+        in h, u, the tracers or the ocean's edge thickness."""
+        check(lib().mpaso_state_check_finite(self._h))
+
     def get(self, field, out=None):
         out = np.empty(self._shape(field)) if out is None else out
         check(lib().mpaso_state_get(self._h, int(field), _ptr(out)))
