@@ -247,6 +247,32 @@ def gpu_arm(args, cfg):
            "path": "mpaso_rk4_step_host (C ABI, pinned host buffers, copy in -> 1 step -> copy out)"
            if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)"}
 
+    # ---- conservation and bounds over an untimed trajectory from the initial state
+    Kd = min(K, 200)
+    for f, a in fields:
+        st.set(f, a)
+    st.step_graph(dt, Kd)
+    st.check_finite()
+    area = mesh.fields["areaCell"][:, None]
+    hN, trN = st.get(G.FIELD_H), st.get(G.FIELD_TRACERS)
+    if app == G.APP_SW:  # thickness-weighted tracer content
+        c0 = (area[..., None] * h[..., None] * tr).sum(axis=(0, 1))
+        cN = (area[..., None] * hN[..., None] * trN).sum(axis=(0, 1))
+    else:  # prescribed constant thickness: the tracer content per area
+        c0 = (area[..., None] * tr).sum(axis=(0, 1))
+        cN = (area[..., None] * trN).sum(axis=(0, 1))
+    lo, hi = tr.min(axis=(0, 1)), tr.max(axis=(0, 1))
+    tol = 1e-12 * (hi - lo)
+    diagnostics = {
+        "steps": Kd,
+        "mass_rel_drift": float(abs((area * hN).sum() - (area * h).sum()) / (area * h).sum()),
+        "tracer_content_rel_drift": [float(abs(x - y) / abs(y)) for x, y in zip(cN, c0)],
+        "tracer_range_initial": [[float(x), float(y)] for x, y in zip(lo, hi)],
+        "tracer_range_final": [[float(x), float(y)] for x, y in zip(trN.min(axis=(0, 1)), trN.max(axis=(0, 1)))],
+        "cells_outside_initial_range": int(((trN < lo - tol) | (trN > hi + tol)).sum()),
+        "finite": True,
+    }
+
     out = None
     if rank == 0:
         cpu = cpu_baseline(cfg, mesh, fct, state) if (world == 1 and not args.no_cpu_baseline) else None
@@ -264,7 +290,7 @@ def gpu_arm(args, cfg):
                        "launch": dict(launch, autotuned=not args.no_autotune)},
             "roofline": roofline, "fp64": fp64, "step_hbm": step_hbm,
             "kernels_ms_per_launch": {k: round(v, 5) for k, v in prof.items()},
-            "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu,
+            "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu, "diagnostics": diagnostics,
             "gpu_launches": st.launches_per_step() * K,
         }
     st.close()
