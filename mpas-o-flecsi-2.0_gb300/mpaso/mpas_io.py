@@ -17,6 +17,11 @@
   one record per output time of h, h_s, vorticity, potential_vorticity and
   tracers along the Time dimension.  Records are read from the device with
   the state's asynchronous snapshots, so writing record n overlaps stepping.
+- `write_restart(path, state, time)` / `read_restart(path, state)`: the
+  prognostic state (h, u, tracers; the ocean's edge thickness) in one file,
+  so a run resumes where it stopped.  The reference has no restart read
+  (its only file output is the history above); resuming from this file
+  continues the trajectory bit for bit.
 """
 import ctypes
 
@@ -408,3 +413,62 @@ class History:
 
     def __exit__(self, *exc):
         self.close()
+
+
+_RESTART_VARS = (  # (variable, field attribute of mpaso.gpu, entity dimension, ocean only)
+    ("h", "FIELD_H", "nCells", False),
+    ("u", "FIELD_U", "nEdges", False),
+    ("layerThicknessEdge", "FIELD_LAYER_THICKNESS_EDGE", "nEdges", True),
+)
+
+
+def write_restart(path, state, time=0.0, version=5):
+    """Writes the state's prognostic fields (reference numbering) and the model time."""
+    import mpaso.gpu as G
+    dm = state.dmesh
+    ocean = state.app == G.APP_OCEAN
+    with NcFile(path, "w", version) as f:
+        for d, n in (("nCells", dm.nC), ("nEdges", dm.nE), ("nVertLevels", state.L),
+                     ("nTracers", max(state.T, 1))):
+            f.def_dim(d, n)
+        f.put_att("app", "ocean" if ocean else "sw")
+        f.put_att("nTracersInState", int(state.T))
+        f.put_att("model_time_s", float(time))
+        for name, _, ent, oc in _RESTART_VARS:
+            if oc and not ocean:
+                continue
+            f.def_var(name, NC_DOUBLE, [ent, "nVertLevels"])
+        if state.T:
+            f.def_var("tracers", NC_DOUBLE, ["nCells", "nVertLevels", "nTracers"])
+        f.enddef()
+        for name, field, _, oc in _RESTART_VARS:
+            if oc and not ocean:
+                continue
+            f.put_var(name, state.get(getattr(G, field)))
+        if state.T:
+            f.put_var("tracers", state.get(G.FIELD_TRACERS))
+
+
+def read_restart(path, state):
+    """Sets the state from a restart file (its mesh sizes, levels, tracers and
+    app must match); returns the model time stored with it."""
+    import mpaso.gpu as G
+    dm = state.dmesh
+    ocean = state.app == G.APP_OCEAN
+    with NcFile(path) as f:
+        dims = f.dims()
+        want = {"nCells": dm.nC, "nEdges": dm.nE, "nVertLevels": state.L}
+        for d, n in want.items():
+            if dims.get(d) != n:
+                raise ValueError(f"restart file has {d} = {dims.get(d)}, the state {n}")
+        if f.get_att("app") is None or f.get_att("nTracersInState") is None:
+            raise ValueError(f"{path} is not a restart file")
+        if f.get_att("app") != ("ocean" if ocean else "sw") or int(f.get_att("nTracersInState")) != state.T:
+            raise ValueError("restart file was written by another app or tracer count")
+        for name, field, _, oc in _RESTART_VARS:
+            if oc and not ocean:
+                continue
+            state.set(getattr(G, field), f.get_var(name))
+        if state.T:
+            state.set(G.FIELD_TRACERS, f.get_var("tracers"))
+        return float(f.get_att("model_time_s"))
