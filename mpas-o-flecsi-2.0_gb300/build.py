@@ -10,6 +10,7 @@ host-only entry points work there) and on the GB300 machine after a rebuild.
 import concurrent.futures as cf
 import hashlib
 import os
+import shutil
 import subprocess
 import sys
 
@@ -21,6 +22,9 @@ LIB = os.path.join(HERE, "lib", "libmpaso.so")
 INC = [os.path.join(ROOT, "include"), CSRC]
 
 NVCC = os.environ.get("NVCC", "nvcc")
+# the toolkit's headers for the g++-compiled sources (NVTX3 is header-only)
+CUDA_INC = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(
+    shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc"))), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 # Per-file extra flags: the per-task kernels keep every multiply and add
@@ -57,7 +61,7 @@ def _compile(src, hdr_digest, verbose):
     if src.endswith(".cu"):
         cmd = [NVCC] + flags + [f"-I{i}" for i in INC] + ["-c", path, "-o", obj]
     else:
-        cmd = ["g++"] + flags + [f"-I{i}" for i in INC] + ["-c", path, "-o", obj]
+        cmd = ["g++"] + flags + [f"-I{i}" for i in INC + [CUDA_INC]] + ["-c", path, "-o", obj]
     if verbose:
         print(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -83,7 +87,7 @@ def build(force=False, verbose=False):
     objs = [o for o, _ in results]
     changed = any(c for _, c in results) or not os.path.exists(LIB)
     if changed:
-        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread"]
+        cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread", "-ldl"]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

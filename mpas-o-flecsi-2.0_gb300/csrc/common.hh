@@ -11,6 +11,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "mpaso_mesh.h"
 
 namespace mpaso {
@@ -63,8 +65,14 @@ template <class F> void parallel_for(int64_t n, F &&f, int64_t grain = 1 << 14) 
   if (ep) std::rethrow_exception(ep);
 }
 
-// Runs `body` and maps exceptions to MPASO_ERR_* codes + the thread-local message.
+// Runs `body` and maps exceptions to MPASO_ERR_* codes + the thread-local
+// message.  Every C-ABI call is an NVTX range named after the entry point
+// (seen by Nsight tools and `ncu --nvtx`; a pointer check when none is attached).
 template <class F> int guarded(const char *where, F &&body) {
+  nvtxRangePushA(where);
+  struct Pop {
+    ~Pop() { nvtxRangePop(); }
+  } pop;
   try {
     body();
     return MPASO_OK;
