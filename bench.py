@@ -777,7 +777,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)  # the workload's 1000 RK4 steps (0.4 s timed)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="sw_l7", choices=sorted(CONFIGS) + ["adjoint_l6", "ensemble"])
+    ap.add_argument("--config", default="sw_l7",
+                    choices=sorted(CONFIGS) + ["adjoint_l6", "adjoint_ocean_l6", "ensemble"])
     ap.add_argument("--adj-steps", type=int, default=500)
     ap.add_argument("--adj-ckpt", type=int, default=25)
     ap.add_argument("--adj-dirs", type=int, default=32)
@@ -794,6 +795,12 @@ def main():
         log("note: fewer than 3 warm-up steps")
     if args.config == "adjoint_l6":
         out = adjoint_arm(args)
+    elif args.config == "adjoint_ocean_l6":
+        leg = ocean_adjoint_leg(args)
+        out = {"metric": "adjoint/forward time ratio (ocean tracer RK4, level-6 sphere, 60 levels x 3 tracers)",
+               "value": leg["ratio"], "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "steps": 20,
+               "dtype": "f64", "data": "synthetic (seeded smooth fields, temperature unclipped)",
+               "config": {"workload": leg["workload"]}, **{k: v for k, v in leg.items() if k != "workload"}}
     elif args.config == "ensemble":
         out = ensemble_arm(args)
     else:

@@ -10,6 +10,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -144,6 +145,21 @@ __device__ __forceinline__ bool dlt0(double x) { return dbits(x) < 0 && dbits(x)
 
 }  // namespace mpaso
 
+// A mesh context is shared by the states made on it: mpaso_mesh_destroy drops
+// the caller's reference and the context is freed with the last reference,
+// so states and their mesh may be destroyed in either order.
 struct mpaso_mesh_s {
   mpaso::MeshCtx ctx;
+  std::atomic<int> refs{1};
 };
+
+namespace mpaso {
+// Drops one reference; frees the context (on its device) with the last one.
+inline void release_mesh(mpaso_mesh_s *m) {
+  if (m->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(m->ctx.device);
+  cudaStreamSynchronize(m->ctx.stream);
+  delete m;
+  cudaGetLastError();  // teardown is best effort: leave no error pending for later calls
+}
+}  // namespace mpaso

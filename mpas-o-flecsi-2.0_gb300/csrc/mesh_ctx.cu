@@ -710,10 +710,7 @@ int mpaso_mesh_create(const mpaso_mesh_desc *desc, int device, mpaso_mesh *out) 
 
 int mpaso_mesh_destroy(mpaso_mesh m) {
   return mpaso::guarded("mpaso_mesh_destroy", [&] {
-    if (!m) return;
-    cudaSetDevice(m->ctx.device);
-    cudaStreamSynchronize(m->ctx.stream);
-    delete m;
+    if (m) mpaso::release_mesh(m);
   });
 }
 

@@ -833,6 +833,7 @@ int mpaso_state_create(mpaso_mesh m, const mpaso_params *p, mpaso_state *out) {
       delete h;
       throw;
     }
+    m->refs.fetch_add(1);  // released by mpaso_state_destroy
     *out = h;
   });
 }
@@ -840,11 +841,14 @@ int mpaso_state_create(mpaso_mesh m, const mpaso_params *p, mpaso_state *out) {
 int mpaso_state_destroy(mpaso_state s) {
   return guarded("mpaso_state_destroy", [&] {
     if (!s) return;
-    cudaSetDevice(s->s.mesh->ctx.device);
+    mpaso_mesh m = s->s.mesh;  // alive: the state holds a reference
+    cudaSetDevice(m->ctx.device);
     cudaStreamSynchronize(s->s.stream);
     cudaStream_t st = s->s.stream;
     delete s;
     cudaStreamDestroy(st);
+    cudaGetLastError();  // teardown is best effort: leave no error pending for later calls
+    release_mesh(m);
   });
 }
 

@@ -144,3 +144,20 @@ def test_calls_out_of_order_and_null_handles():
     assert lib().mpaso_state_check_finite(None) == 1
     st.step(60.0, 1)  # the state is still usable
     st.check_finite()
+
+
+def test_mesh_destroyed_before_its_state():
+    """A mesh context outlives its destroy call while states use it (Python may
+    finalise a state and its mesh in either order when they die in a cycle):
+    the state keeps stepping, and tearing both down leaves no CUDA error
+    behind for the next call."""
+    import mpaso.gpu as G
+    mesh = mpaso.Mesh.icosa(2)
+    dm = G.DeviceMesh(mesh, fct=fct_statics(mesh, 1))
+    st = G.State(dm, nlev=1, ntr=1, fct=True)
+    st.set(G.FIELD_H, np.full((mesh.nCells, 1), 1000.0))
+    dm.close()
+    st.step(60.0, 3)
+    st.check_finite()
+    st.close()
+    fct_statics(mesh, 1, device=0)  # a later call's own error check sees nothing stale
