@@ -79,6 +79,8 @@ typedef struct {
 
 /* Builds the device mesh context on `device` (-1 = current device). */
 int mpaso_mesh_create(const mpaso_mesh_desc *desc, int device, mpaso_mesh *out);
+/* Drops the caller's reference: the context is freed when it and every state
+ * made on it (mpaso_state_create) have been destroyed, in any order. */
 int mpaso_mesh_destroy(mpaso_mesh m);
 /* new_to_old[new] = reference id, for MPASO_CELLS/EDGES/VERTICES. */
 int mpaso_mesh_permutation(mpaso_mesh m, int32_t entity, int32_t *new_to_old);
