@@ -228,6 +228,18 @@ def gpu_arm(args, cfg):
             st.step_host(dt, 1, hp, up, tp)
         a1.record(ext)
         a1.synchronize()
+        blocking_ms = a0.elapsed_time(a1)
+        # the same calls queued (mpaso_rk4_step_host_async): each still copies its
+        # inputs in from and its results out to the page-locked buffers, in order,
+        # but the host does not wait in between; one sync at the end
+        st.step_host_async(dt, 1, hp, up, tp)
+        st.sync()
+        a0.record(ext)
+        for _ in range(Ke):
+            st.step_host_async(dt, 1, hp, up, tp)
+        a1.record(ext)
+        st.sync()
+        a1.synchronize()
         e2e_ms = a0.elapsed_time(a1)
     else:
         tp = pin(tr)
@@ -244,8 +256,13 @@ def gpu_arm(args, cfg):
     e2e_max = reduce_over_ranks(e2e_ms, "max", device="cuda")
     e2e = {"value": world * units_rank * Ke / (e2e_max * 1e-3), "unit": "cell-updates/s",
            "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
-           "path": "mpaso_rk4_step_host (C ABI, pinned host buffers, copy in -> 1 step -> copy out)"
+           "path": "mpaso_rk4_step_host_async x steps, then mpaso_state_sync (C ABI, pinned host buffers: "
+                   "copy in -> 1 step -> copy out every step)"
            if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)"}
+    if app == G.APP_SW:
+        bl = reduce_over_ranks(blocking_ms, "max", device="cuda")
+        e2e["blocking"] = {"value": world * units_rank * Ke / (bl * 1e-3),
+                           "path": "mpaso_rk4_step_host, which returns after each step's copy out"}
 
     # ---- conservation and bounds over an untimed trajectory from the initial state
     Kd = min(K, 200)

@@ -242,6 +242,13 @@ int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps);
 /* One call through the boundary with host buffers: copy in, nsteps, copy out. */
 int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
                         double *tracers);
+/* The same exchange queued on the state's stream without waiting for it
+ * (page-locked buffers only): calls run in order, each copying in what the
+ * previous one copied out, so a time loop of these keeps the GPU busy while
+ * the host returns at once.  The buffers must not be touched until
+ * mpaso_state_sync returns. */
+int mpaso_rk4_step_host_async(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                              double *tracers);
 int mpaso_state_sync(mpaso_state s);
 /* History output without stalling the time loop (the reference writes each
  * output step synchronously: the field_output_wrapper task of apps/sw/run.cc:10

@@ -1012,9 +1012,12 @@ int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps) {
   });
 }
 
-int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
-                        double *tracers) {
-  return guarded("mpaso_rk4_step_host", [&] {
+namespace {
+// The host-buffer exchange of mpaso_rk4_step_host[_async]; `wait` = return
+// after the results are in the host buffers, else right after the launch
+// (page-locked buffers only).
+void step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u, double *tracers, bool wait) {
+  {
     require(s && h && u && nsteps >= 0, MPASO_ERR_ARG, "bad argument");
     SwState &S = s->s;
     MeshCtx &ctx = S.mesh->ctx;
@@ -1033,10 +1036,11 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
       if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) locked = false;
       cudaGetLastError();
     }
+    require(wait || locked, MPASO_ERR_ARG, "the asynchronous exchange needs page-locked host buffers");
     const XKey key{h, u, tr ? tracers : nullptr, dt, nsteps};
     if (locked && S.xg && S.xkey == key) {
       MPASO_CUDA(cudaGraphLaunch(S.xg, st));
-      MPASO_CUDA(cudaStreamSynchronize(st));
+      if (wait) MPASO_CUDA(cudaStreamSynchronize(st));
       return;
     }
     if (S.xg) {
@@ -1146,8 +1150,19 @@ int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, dou
       S.xkey = key;
       MPASO_CUDA(cudaGraphLaunch(S.xg, st));
     }
-    MPASO_CUDA(cudaStreamSynchronize(st));
-  });
+    if (wait) MPASO_CUDA(cudaStreamSynchronize(st));
+  }
+}
+}  // namespace
+
+int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                        double *tracers) {
+  return guarded("mpaso_rk4_step_host", [&] { step_host(s, dt, nsteps, h, u, tracers, true); });
+}
+
+int mpaso_rk4_step_host_async(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
+                              double *tracers) {
+  return guarded("mpaso_rk4_step_host_async", [&] { step_host(s, dt, nsteps, h, u, tracers, false); });
 }
 
 }  // extern "C"

@@ -268,6 +268,11 @@ class State:
         check(lib().mpaso_rk4_step_host(self._h, ctypes.c_double(dt), int(nsteps), _ptr(h), _ptr(u),
                                         _ptr(tracers)))
 
+    def step_host_async(self, dt, nsteps, h, u, tracers):
+        """The same exchange queued without waiting (page-locked buffers; read them after sync())."""
+        check(lib().mpaso_rk4_step_host_async(self._h, ctypes.c_double(dt), int(nsteps), _ptr(h), _ptr(u),
+                                              _ptr(tracers)))
+
     def sync(self):
         check(lib().mpaso_state_sync(self._h))
 

@@ -180,6 +180,27 @@ def test_host_boundary_call_with_page_locked_buffers():
     assert np.array_equal(hp.numpy(), h) and np.array_equal(up.numpy(), u) and np.array_equal(tp.numpy(), tr)
 
 
+def test_async_host_boundary_calls_in_a_loop():
+    """Queued one-step exchanges on the same page-locked buffers (each copying in
+    what the previous one copied out) end where the same number of blocking
+    calls ends, bit for bit; pageable buffers are refused for the queued form."""
+    torch = pytest.importorskip("torch")
+    g = Golden("sw_fct_icosa3_L1T1")
+    _, st = make_state(g)
+    h, u, tr = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (g["h0"], g["u0"], g["tr0"]))
+    for _ in range(5):
+        st.step_host(g.dt, 1, h, u, tr)
+    _, st2 = make_state(g)
+    ha, ua, ta = (torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in (g["h0"], g["u0"], g["tr0"]))
+    for _ in range(5):
+        st2.step_host_async(g.dt, 1, ha, ua, ta)
+    st2.sync()
+    for a, b in ((h, ha), (u, ua), (tr, ta)):
+        assert np.array_equal(a.numpy(), b.numpy())
+    with pytest.raises(mpaso.MpasoError, match="page-locked"):
+        st2.step_host_async(g.dt, 1, g["h0"].copy(), g["u0"].copy(), g["tr0"].copy())
+
+
 def test_history_snapshots_while_stepping():
     """Snapshots taken between graph-replayed steps, copied out asynchronously while
     later steps run, equal the state read synchronously at the same points."""
