@@ -84,6 +84,7 @@ struct DMesh {
 // Host-side mesh context.
 struct MeshCtx {
   int device = 0;
+  int sms = 152;  // streaming multiprocessors of `device` (set when the context is built)
   cudaStream_t stream = nullptr;
   double gravity = 9.80616;  // mpasoflecsi/common/constants.hh:370-371
   bool has_fct = false;

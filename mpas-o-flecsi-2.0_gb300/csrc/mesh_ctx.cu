@@ -639,6 +639,7 @@ int mpaso_mesh_create_ensemble(const mpaso_mesh_desc *members, int32_t n, int de
     auto *h = new mpaso_mesh_s();
     try {
       h->ctx.device = device;
+      MPASO_CUDA(cudaDeviceGetAttribute(&h->ctx.sms, cudaDevAttrMultiProcessorCount, device));
       MPASO_CUDA(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking));
       mpaso::build(h->ctx, U.u, &U.mcells);
       for (int i = 0; i <= n; ++i)
@@ -698,6 +699,7 @@ int mpaso_mesh_create(const mpaso_mesh_desc *desc, int device, mpaso_mesh *out) 
     auto *h = new mpaso_mesh_s();
     try {
       h->ctx.device = device;
+      MPASO_CUDA(cudaDeviceGetAttribute(&h->ctx.sms, cudaDevAttrMultiProcessorCount, device));
       MPASO_CUDA(cudaStreamCreateWithFlags(&h->ctx.stream, cudaStreamNonBlocking));
       mpaso::build(h->ctx, *desc);
     } catch (...) {
