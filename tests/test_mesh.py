@@ -94,3 +94,19 @@ def test_sfc_reorder_is_permutation(sphere):
     f, g = sphere.fields, r.fields
     assert np.array_equal(g["xCell"], f["xCell"][pc])
     assert np.allclose(g["areaCell"], f["areaCell"][pc], rtol=1e-13)
+
+
+def test_crs_is_cached_until_a_connectivity_array_is_replaced():
+    """Mesh.crs() is built once and shared; replacing one of the file's
+    connectivity arrays rebuilds it from the new array."""
+    m = mpaso.Mesh.icosa(2)
+    a = m.crs()
+    assert m.crs() is a
+    coc = m.fields["cellsOnCell"].copy()
+    coc[0, [0, 1]] = coc[0, [1, 0]]  # swap two neighbours of cell 0
+    m.fields["cellsOnCell"] = coc
+    b = m.crs()
+    assert b is not a
+    off, idx = b["c2c"]
+    assert np.array_equal(idx[off[0]:off[0] + 2], a["c2c"][1][[1, 0]])
+    assert np.array_equal(b["e2e"][1], a["e2e"][1])
