@@ -55,3 +55,25 @@ def test_planar_second_derivative_exact_for_quadratics():
     n = s["nAdvCellsForEdge"]
     tot = np.array([s["advCoef"][e, :n[e]].sum() for e in range(m.nEdges)])
     assert np.allclose(tot, f["dvEdge"], rtol=1e-9)
+
+
+def test_batched_device_setup_validates_members_on_the_host():
+    """mpaso_fct_setup_device_many checks every member's offsets and indices
+    before any device work, so a corrupted member is refused, by number, even
+    on a host without a GPU."""
+    import types
+
+    import mpaso
+    from mpaso._lib import MpasoError
+    from mpaso.setup import fct_statics_many
+    good = mpaso.Mesh.icosa(1)
+    bad_src = mpaso.Mesh.icosa(1)
+    crs = dict(bad_src.crs())
+    off, idx = crs["c2c"]
+    idx = idx.copy()
+    idx[3] = bad_src.nCells + 1
+    crs["c2c"] = (off, idx)
+    bad = types.SimpleNamespace(crs=lambda: crs, fields=bad_src.fields, nCells=bad_src.nCells,
+                                nEdges=bad_src.nEdges, nVertices=bad_src.nVertices, on_sphere=True)
+    with pytest.raises(MpasoError, match="member 1: cell index out of range"):
+        fct_statics_many([good, bad], 1, device=0)
