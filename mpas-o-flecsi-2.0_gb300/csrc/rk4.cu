@@ -23,6 +23,9 @@
 // rcp_nr.  Results match the reference task sequence to rounding (about 1e-15
 // relative per step), not bit for bit.
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "rk4.cuh"
 
@@ -441,16 +444,29 @@ void launch_ex(void (*kern)(A...), int64_t n, int b, bool win, const SwState &s,
   MPASO_CUDA(cudaLaunchKernelEx(&cfg, kern, m, d, S, L));
 }
 
+// Blocks of `b` threads of `kern` that one SM holds at once (cached per
+// kernel and block size: the query is not free and launches repeat).
+template <class K> int resident_blocks(K kern, int b) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> cache;
+  const auto key = std::make_pair((const void *)kern, b);
+  std::lock_guard<std::mutex> g(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  MPASO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, b, 0));
+  return cache[key] = std::max(nb, 1);
+}
+
 template <int T, int OC>
 void launch_k1(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
   const int64_t n = (int64_t)m.nE * s.L;
   const bool win = s.tune_l2 == 1;
-  const int64_t nres = std::min<int64_t>(n, (int64_t)s.mesh->ctx.sms * (1536 / b) * b);  // resident threads
-  if (unroll)
-    launch_ex(k_sw_edge_pre<T, 10, OC>, nres, b, win, s, st, m, s.st, S, s.L);
-  else
-    launch_ex(k_sw_edge_pre<T, 0, OC>, nres, b, win, s, st, m, s.st, S, s.L);
+  auto kern = unroll ? k_sw_edge_pre<T, 10, OC> : k_sw_edge_pre<T, 0, OC>;
+  // the grid-stride kernel runs on exactly the threads the SMs hold at once
+  const int64_t nres = std::min<int64_t>(n, (int64_t)s.mesh->ctx.sms * resident_blocks(kern, b) * b);
+  launch_ex(kern, nres, b, win, s, st, m, s.st, S, s.L);
 }
 
 template <int T, int OC, int SPLIT>
