@@ -759,7 +759,7 @@ def reference_arm(args, cfg):
         except OSError:
             kind = "port"
     steps = max(1, min(args.steps, args.ref_max_steps))
-    warm = min(args.warmup, 1)
+    warm = min(args.warmup, 3)  # untimed warm-up steps per process (~0.4 s each at level 7)
     cores = args.ref_procs or (os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
     mgr = ctx.Manager()
