@@ -269,12 +269,14 @@ __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
 }
 
 // Initial diagnostics (apps/sw/run.cc:226-230).
+// NC = 6: the cell loops unrolled for meshes of at most hexagons (as k_sw_final's unrolled variant)
+template <int NC>
 __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int L) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nCL = (int64_t)m.nC * L;
   if (i < nCL) {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    cell_diag<0>(m, st, S, L, c, k, i, S.u_in);
+    cell_diag<NC>(m, st, S, L, c, k, i, S.u_in);
     return;
   }
   i -= nCL;
@@ -554,7 +556,10 @@ void ensure_diag(SwState &s, cudaStream_t st) {
   if (s.diag_valid) return;
   const DMesh &m = s.mesh->ctx.d;
   Stage S = make_stage(s, 0, 0.0);
-  k_sw_diag<<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+  if (m.maxEoC <= 6)
+    k_sw_diag<6><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+  else
+    k_sw_diag<0><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
   MPASO_CUDA(cudaGetLastError());
   s.diag_valid = true;
 }
@@ -622,7 +627,10 @@ void sw_diag_ptrs(SwState &s, const double *u, const double *h, double *tape_pv,
   Stage S = make_stage(s, 0, 0.0);
   S.u_in = u, S.h_in = h;
   S.tape_pv = tape_pv, S.tape_hs = tape_hs;
-  k_sw_diag<<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+  if (m.maxEoC <= 6)
+    k_sw_diag<6><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
+  else
+    k_sw_diag<0><<<blocks_for(((int64_t)m.nC + m.nV) * s.L, TPB), TPB, 0, st>>>(m, s.st, S, s.L);
 }
 
 void sw_steps_pub(SwState &s, double dt, int nsteps, cudaStream_t st) { sw_steps(s, dt, nsteps, st); }
