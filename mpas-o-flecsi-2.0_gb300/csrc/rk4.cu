@@ -817,6 +817,10 @@ double *ensure_io(SwState &S, size_t bytes) {
       MPASO_CUDA(cudaStreamSynchronize(S.stream));
       MPASO_CUDA(cudaFree(S.io_stage));
     }
+    if (S.xg) {  // the captured host exchange holds the old staging addresses
+      MPASO_CUDA(cudaGraphExecDestroy(S.xg));
+      S.xg = nullptr;
+    }
     S.io_stage = nullptr, S.io_bytes = 0;
     if (cudaMalloc((void **)&S.io_stage, bytes) != cudaSuccess) {
       cudaGetLastError();
