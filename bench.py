@@ -183,7 +183,6 @@ def gpu_arm(args, cfg):
     top = max(prof, key=prof.get)
     prof_total = sum(prof.values())
     peak, peak_kind = measured_peaks()
-    fp64_peak = G.probe_fp64(local)
     kb, kf = model[top]
     achieved = kb / (prof[top] * 1e-3) / 1e9
     traffic = None
@@ -206,7 +205,6 @@ def gpu_arm(args, cfg):
     fp64 = {"achieved_per_s": kf / (prof[top] * 1e-3), "peak_per_s": pipe_peak,
             "frac": round(kf / (prof[top] * 1e-3) / pipe_peak, 4), "kernel": top,
             "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / pipe_peak, 4),
-            "dfma_chain_probe_per_s": fp64_peak,
             "note": "FP64 instructions per launch from mpaso/perfmodel.py (within ~10% of ncu's counts) "
                     "/ measured launch time, against the FP64 pipe peak of 2 per clock per SM"}
     step_hbm = {"algorithmic_bytes_per_step": int(step_bytes),

@@ -128,9 +128,12 @@ int mpaso_sw_compute_tend(mpaso_mesh m, int32_t nlev, const double *h_edge, cons
  * synchronisation).  All seven arrays must be device memory.  Arguments are
  * staged through one static 32 MiB device array instead of allocated scratch,
  * which limits the mesh to (4 nEdges + 3 nCells) * nlev <= 4,194,304 doubles
- * (larger meshes get MPASO_ERR_ARG).  The first call on a device looks up that
- * array's address (cudaGetSymbolAddress): make it before any stream capture.
- * Every call shares the array, so calls whose GPU work overlaps race. */
+ * (larger meshes get MPASO_ERR_ARG).  Each call looks up that array's
+ * address (cudaGetSymbolAddress) unless its stream is being captured, when it
+ * reuses the address of the last uncaptured call on that device: make the
+ * first call on each device before any stream capture.  The array is not
+ * counted by mpaso_mesh_device_bytes.  Every call shares the array, so calls
+ * whose GPU work overlaps race. */
 int mpaso_sw_compute_tend_noalloc(mpaso_mesh m, int32_t nlev, const double *h_edge,
                                   const double *h, const double *u, const double *ke,
                                   const double *pv_edge, double *tend_h, double *tend_u,
@@ -343,10 +346,6 @@ int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0
 int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, const double *gtr,
                           double *gh0, double *gu0, double *gtr0);
 int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);
-
-/* FP64 ceiling of `device`: DFMA lane-operations per second issued by a
- * compute-only probe kernel (GB300 runs FP64 at a small fraction of FP32). */
-int mpaso_probe_fp64(int device, double *dfma_per_s);
 
 /* Device / runtime queries (no GPU needed: report 0 devices). */
 int mpaso_device_count(int32_t *n);

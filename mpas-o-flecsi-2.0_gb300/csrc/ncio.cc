@@ -95,7 +95,24 @@ uint64_t get_be(const uint8_t *p, int n) {
 struct Reader {
   NcFile &f;
   int64_t pos = 0;
-  explicit Reader(NcFile &file) : f(file) {}
+  int64_t size = 0;  // bytes in the file
+  explicit Reader(NcFile &file) : f(file) {
+    const long at = ftell(f.fp);
+    if (at < 0 || fseek(f.fp, 0, SEEK_END) != 0) io_fail(f, "cannot size the file");
+    size = (int64_t)ftell(f.fp);
+    if (size < 0 || fseek(f.fp, at, SEEK_SET) != 0) io_fail(f, "cannot size the file");
+    pos = at;
+  }
+  // Bytes of a count or size field (NON_NEG: 4, 8 in CDF-5).
+  int nn() const { return f.version == 5 ? 8 : 4; }
+  // Refuses a count read from the header whose entries, at `each` bytes at
+  // least, could not fit in what is left of the file -- before any vector is
+  // sized by it, so a corrupt or truncated header costs no large allocation.
+  int64_t fits(int64_t n, int64_t each, const char *what) {
+    const int64_t left = size - pos;
+    if (n < 0 || (each > 0 && n > left / each)) io_fail(f, std::string("truncated or corrupt header (") + what + ")");
+    return n;
+  }
   void bytes(void *dst, int64_t n) {
     if (n > 0 && fread(dst, 1, (size_t)n, f.fp) != (size_t)n) io_fail(f, "truncated header");
     pos += n;
@@ -135,7 +152,8 @@ struct Reader {
     return n;
   }
   std::vector<Att> atts() {
-    std::vector<Att> out((size_t)list(kAttTag));
+    // an attribute takes at least a name (count + 4), a type and a count
+    std::vector<Att> out((size_t)fits(list(kAttTag), 2 * nn() + 8, "attribute count"));
     for (Att &a : out) {
       a.name = name();
       a.type = (int32_t)be(4);
@@ -143,6 +161,7 @@ struct Reader {
       if (!ts || (a.type == MPASO_NC_INT64 && f.version != 5)) io_fail(f, "bad attribute type");
       a.n = nonneg();
       if (a.n < 0 || a.n > (int64_t)1 << 30) io_fail(f, "attribute too large");
+      fits(a.n, ts, "attribute length");
       a.be.resize((size_t)(a.n * ts));
       bytes(a.be.data(), (int64_t)a.be.size());
       skip(pad4((int64_t)a.be.size()) - (int64_t)a.be.size());
@@ -182,7 +201,8 @@ void read_header(NcFile &f) {
   const uint64_t nr = r.be(f.version == 5 ? 8 : 4);
   const bool streaming = f.version == 5 ? nr == ~0ULL : nr == kStreaming;
   f.numrecs = streaming ? -1 : (int64_t)nr;
-  f.dims.resize((size_t)r.list(kDimTag));
+  // a dimension takes at least a name (count + 4) and a length
+  f.dims.resize((size_t)r.fits(r.list(kDimTag), 2 * r.nn() + 4, "dimension count"));
   int nrecdims = 0;
   for (Dim &d : f.dims) {
     d.name = r.name();
@@ -191,11 +211,14 @@ void read_header(NcFile &f) {
   }
   if (nrecdims > 1) io_fail(f, "more than one record dimension");
   f.gatts = r.atts();
-  f.vars.resize((size_t)r.list(kVarTag));
+  // a variable takes at least a name (count + 4), a dimension count, an empty
+  // attribute list (tag + count), a type, a size and a 4-byte offset
+  f.vars.resize((size_t)r.fits(r.list(kVarTag), 4 * r.nn() + 16, "variable count"));
   for (Var &v : f.vars) {
     v.name = r.name();
     const int64_t nd = r.nonneg();
     if (nd > 64) io_fail(f, "too many dimensions");
+    r.fits(nd, r.nn(), "dimension ids");
     v.dims.resize((size_t)nd);
     for (int32_t &d : v.dims) {
       const int64_t id = r.nonneg();

@@ -12,11 +12,16 @@
 //
 // The array is a file-scope __device__ buffer of kScratchDoubles doubles
 // (32 MiB).  Every GPU that loads the library holds it until the process
-// exits.  Host code cannot use the symbol itself as a device address, so the
-// first call on each device (with that device current) asks the runtime for
-// its address once with cudaGetSymbolAddress and caches it; make that first
-// call before any stream capture.  All calls share the one array: calls whose
-// GPU work overlaps (different streams, different host threads) race on it.
+// exits.  Host code cannot use the symbol itself as a device address, so each
+// call (with the context's device current) asks the runtime for the address
+// with cudaGetSymbolAddress -- a cheap lookup -- and keeps it per device.  A
+// call made while its stream is being captured uses the kept address instead
+// (the lookup may load the module, which a capture does not allow), so make
+// the first call on each device before any stream capture.  Looking the
+// address up again on every uncaptured call keeps it right after a
+// cudaDeviceReset, which reloads the module and may move the array.  All calls
+// share the one array: calls whose GPU work overlaps (different streams,
+// different host threads) race on it.
 #include <mutex>
 
 #include "task_io.cuh"
@@ -36,20 +41,27 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double *g_addr[kMaxDevices] = {};
 
-// Device address of g_scratch on `device` (which must be current).
-double *scratch_address(int device) {
+// Device address of g_scratch on `device` (which must be current): looked up
+// afresh unless `s` is capturing, in which case the address kept from the
+// last uncaptured call on this device is used.
+double *scratch_address(int device, cudaStream_t s) {
   require(device >= 0 && device < kMaxDevices, MPASO_ERR_ARG, "device index out of range");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MPASO_CUDA(cudaStreamIsCapturing(s, &cs));
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[device]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      cudaGetLastError();
-      fail(MPASO_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
-                               cudaGetErrorString(e));
-    }
-    g_addr[device] = (double *)p;
+  if (cs != cudaStreamCaptureStatusNone) {
+    require(g_addr[device] != nullptr, MPASO_ERR_ARG,
+            "the first allocation-free call on a device must come before any stream capture");
+    return g_addr[device];
   }
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    cudaGetLastError();
+    fail(MPASO_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
+                             cudaGetErrorString(e));
+  }
+  g_addr[device] = (double *)p;
   return g_addr[device];
 }
 
@@ -81,8 +93,8 @@ extern "C" int mpaso_sw_compute_tend_noalloc(mpaso_mesh m, int32_t nlev, const d
                               " doubles of staging, the static scratch holds " +
                               std::to_string(kScratchDoubles) + " ((4 nEdges + 3 nCells) * nlev must fit)");
     MPASO_CUDA(cudaSetDevice(ctx.device));
-    double *base = scratch_address(ctx.device);
     const cudaStream_t s = stream ? (cudaStream_t)stream : ctx.stream;
+    double *base = scratch_address(ctx.device, s);
     double *s_he = base, *s_u = s_he + nE * L, *s_pve = s_u + nE * L, *s_h = s_pve + nE * L;
     double *s_ke = s_h + nC * L, *s_th = s_ke + nC * L, *s_tu = s_th + nC * L;
     // Every scratch element read below is written earlier in this call (the

@@ -11,6 +11,12 @@
 // geometry, FCT statics): make_mesh_context() builds it once from the mesh
 // specialization after read_fields (apps/sw/initialize.cc:41-61), and
 // mesh_context() is what the task bodies use.
+//
+// Single-color runs only.  The specialization partitions the mesh into one
+// color per process (mpasoflecsi/specialization/mesh.cc:31); with more than
+// one, a color's local connectivity holds partition-edge cells whose stencils
+// reach into ghosts, and the device context has no halo exchange.
+// make_mesh_context() refuses such runs.
 #pragma once
 
 #include <cstdint>
@@ -20,6 +26,7 @@
 #include <utility>
 #include <vector>
 
+#include "flecsi/execution.hh"
 #include "mpaso.h"
 
 namespace mpaso_flecsi {
@@ -69,6 +76,9 @@ template <class Mesh, class DA>
 void make_mesh_context(Mesh &m, DA areaCell, DA dvEdge, DA dcEdge, DA areaTriangle, const double *kiteAreasOnVertex,
                        DA fVertex, const double *weightsOnEdge, const double *bottomDepth, DA xCell, DA yCell,
                        DA zCell, const FctStatics *fct = nullptr, int device = -1) {
+  if (flecsi::processes() != 1)
+    fail("the device mesh context supports single-color runs only (" + std::to_string(flecsi::processes()) +
+         " colors): the per-task wrappers have no halo exchange");
   std::vector<int64_t> off[5];
   std::vector<int32_t> idx[5];  // c2v, c2e, c2c, e2v, e2e
   for (auto &o : off) o.push_back(0);

@@ -61,13 +61,6 @@ def _ptr(a):
     raise TypeError(f"unsupported array type {type(a)}")
 
 
-def probe_fp64(device=0):
-    """DFMA lane-operations per second of the device (live FP64 ceiling)."""
-    v = ctypes.c_double()
-    check(lib().mpaso_probe_fp64(int(device), ctypes.byref(v)))
-    return v.value
-
-
 def device_count():
     n = ctypes.c_int32()
     check(lib().mpaso_device_count(ctypes.byref(n)))

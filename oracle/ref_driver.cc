@@ -2,7 +2,7 @@
 // (compiled unmodified against oracle/shim/): exposes the oracle.h C API,
 // calling the reference task functions on caller memory, and composes them
 // into the reference's RK4 drivers (apps/sw/run.cc:13-70,
-// apps/ocean/run.cc:10-50).  Built by oracle/build_ref.py into
+// apps/ocean/run.cc:10-50).  Built by oracle/build.py (build_ref) into
 // oracle/_ref/libref_L<L>_T<T>.so, one library per compile-time level/tracer
 // count; never shipped, never linked into the product.
 #include <cstring>

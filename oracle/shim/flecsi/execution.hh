@@ -1,12 +1,17 @@
 // Oracle shim (test infrastructure only): program_option stand-in.  The
 // drivers set option values directly (the reference reads them from the CLI).
 #pragma once
+#include <cstddef>
 #include <initializer_list>
 #include <utility>
 
 #include "flecsi/data.hh"
 
 namespace flecsi {
+
+// One process, one color (the specialization makes one color per process,
+// mpasoflecsi/specialization/mesh.cc:31).
+inline std::size_t processes() { return 1; }
 
 struct option_default_t {};
 inline constexpr option_default_t option_default{};

@@ -136,6 +136,32 @@ def test_errors(tmp_path):
         assert e.value.code == 5
 
 
+@pytest.mark.parametrize("version", [1, 2, 5])
+def test_corrupt_header_counts_refused_before_allocating(tmp_path, version):
+    """Counts in a header (dimensions, variables, attributes, attribute
+    lengths) that the rest of the file could not hold are refused as a
+    malformed file, without sizing anything by them."""
+    nn = 8 if version == 5 else 4
+    be = lambda v, n=nn: int(v).to_bytes(n, "big")  # noqa: E731
+    head = b"CDF" + bytes([version]) + be(0)
+    cases = {
+        "dims": head + be(10, 4) + be(2**31 - 1),                      # NC_DIMENSION, huge count
+        "gatts": head + be(0, 4) + be(0) + be(12, 4) + be(2**31 - 1),  # NC_ATTRIBUTE, huge count
+        "vars": head + be(0, 4) + be(0) + be(0, 4) + be(0) + be(11, 4) + be(2**31 - 1),
+        # one global attribute of type double with 2**30 values and 8 bytes of data
+        "attlen": head + be(0, 4) + be(0) + be(12, 4) + be(1) + be(1) + b"a\0\0\0" + be(6, 4)
+                  + be(2**30) + bytes(8),
+    }
+    for name, data in cases.items():
+        p = str(tmp_path / f"{name}.nc")
+        with open(p, "wb") as f:
+            f.write(data + bytes(64))
+        with pytest.raises(MpasoError) as e:
+            NcFile(p)
+        assert e.value.code == 9, name
+        assert "truncated or corrupt header" in str(e.value) or "too large" in str(e.value), (name, str(e.value))
+
+
 @pytest.mark.parametrize("kind,version", [("icosa2", 5), ("hex", 2)])
 def test_mpas_mesh_round_trip(tmp_path, kind, version):
     m = mpaso.Mesh.icosa(2) if kind == "icosa2" else mpaso.Mesh.hex(6, 4, 10e3)

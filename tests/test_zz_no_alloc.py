@@ -30,6 +30,9 @@ def test_noalloc_tend_matches_regular_entry_twice():
     L = 2
     nC, nE = mesh.nCells, mesh.nEdges
     rng = np.random.default_rng(42)
+    # the context's own device memory before any per-task call: the entry under
+    # test runs first on this fresh context and must not grow it
+    bytes0 = dm.device_bytes()
     for call in range(2):
         host = dict(he=900 + 100 * rng.random((nE, L)), h=1000 + 100 * rng.random((nC, L)),
                     u=10 * rng.standard_normal((nE, L)), ke=rng.random((nC, L)),
@@ -39,9 +42,11 @@ def test_noalloc_tend_matches_regular_entry_twice():
                  torch.full((nE, L), np.nan, dtype=torch.float64, device="cuda")) for _ in range(2)]
         torch.cuda.synchronize()
         args = [_ptr(dev[k]) for k in ("he", "h", "u", "ke", "pve")]
-        check(lib().mpaso_sw_compute_tend(dm.handle, L, *args, _ptr(outs[0][0]), _ptr(outs[0][1]), None))
         check(lib().mpaso_sw_compute_tend_noalloc(dm.handle, L, *args, _ptr(outs[1][0]), _ptr(outs[1][1]),
                                                   None))
+        if call == 0:
+            assert dm.device_bytes() == bytes0, "the allocation-free entry grew the context's scratch"
+        check(lib().mpaso_sw_compute_tend(dm.handle, L, *args, _ptr(outs[0][0]), _ptr(outs[0][1]), None))
         torch.cuda.synchronize()  # both entries ran on the context's stream: wait for the device
         ref_h, ref_u = outs[0][0].cpu().numpy(), outs[0][1].cpu().numpy()
         got_h, got_u = outs[1][0].cpu().numpy(), outs[1][1].cpu().numpy()
