@@ -44,8 +44,8 @@ typedef struct mpaso_state_s *mpaso_state;
 /* Mesh description in the reference's terms.  Connectivity is FleCSI's CRS
  * (0-based) in file order: c2v = verticesOnCell, c2e = edgesOnCell,
  * c2c = cellsOnCell, e2v = verticesOnEdge, e2e = edgesOnEdge
- * (mpasoflecsi/specialization/mesh.cc:221-243).  The transposes v2c, e2c, v2e
- * are built inside, as mesh.cc:262-270 builds them (ascending ids). */
+ * (mpasoflecsi/specialization/mesh.cc:67-89).  The transposes v2c, e2c, v2e
+ * are built inside, as mesh.cc:108-116 builds them (ascending ids). */
 typedef struct {
   int64_t nCells, nEdges, nVertices;
   const int64_t *c2v_off, *c2e_off, *c2c_off, *e2v_off, *e2e_off;
@@ -63,7 +63,7 @@ typedef struct {
    * Hilbert curve of their own position; 3 cells in Morton order, edges and
    * vertices after their cells (results agree across orders to rounding) */
   int32_t reorder;
-  /* FCT / del2 statics (apps/ocean/state.hh:261-294); NULL = not available */
+  /* FCT / del2 statics (apps/ocean/state.hh:68-101); NULL = not available */
   int32_t fct_nlev; /* level count of highOrderAdvMask */
   const int32_t *maxLevelCell, *maxLevelEdgeTop, *nAdvCellsForEdge;
   const int32_t *advCellsForEdge;  /* [nE][16] */
@@ -85,7 +85,7 @@ int mpaso_mesh_destroy(mpaso_mesh m);
 /* new_to_old[new] = reference id, for MPASO_CELLS/EDGES/VERTICES. */
 int mpaso_mesh_permutation(mpaso_mesh m, int32_t entity, int32_t *new_to_old);
 /* Gravity used by compute_tend (the reference's mpas_constants::gravity,
- * mpasoflecsi/common/constants.hh:370-371; default 9.80616). */
+ * mpasoflecsi/common/constants.hh:30-31; default 9.80616). */
 int mpaso_mesh_set_gravity(mpaso_mesh m, double gravity);
 /* Bytes of device memory held by the context. */
 int mpaso_mesh_device_bytes(mpaso_mesh m, int64_t *bytes);

@@ -117,7 +117,7 @@ int mpaso_fct_setup(const mpaso_fct_setup_in *in, mpaso_fct_setup_out *out);
 
 /* The same setup computed on GPU `device` (host arrays in and out; the call
  * returns when the outputs are written).  No counterpart in the reference,
- * which runs it on the host at start-up (apps/ocean/initialize.cc:391-400).
+ * which runs it on the host at start-up (apps/ocean/initialize.cc:88-102).
  * One thread per cell fits the second-derivative polynomial and one per edge
  * assembles the advection stencil; offsets and indices are validated on the
  * host first.  Integer outputs equal mpaso_fct_setup's exactly; derivTwo and

@@ -86,7 +86,7 @@ struct MeshCtx {
   int device = 0;
   int sms = 152;  // streaming multiprocessors of `device` (set when the context is built)
   cudaStream_t stream = nullptr;
-  double gravity = 9.80616;  // mpasoflecsi/common/constants.hh:370-371
+  double gravity = 9.80616;  // mpasoflecsi/common/constants.hh:30-31
   bool has_fct = false;
   DMesh d{};
   std::vector<int32_t> perm[3];   // new -> reference id

@@ -20,8 +20,8 @@ namespace mpaso {
 namespace {
 
 constexpr int kME = 8, kME2 = 16, kNA = 6, kMM = kME + 1;
-constexpr double kA = 6371000.0;           // mpasoflecsi/common/constants.hh:368
-constexpr double kPi = 3.141592653589793;  // constants.hh:369
+constexpr double kA = 6371000.0;           // mpasoflecsi/common/constants.hh:28
+constexpr double kPi = 3.141592653589793;  // constants.hh:29
 
 inline double smax(double a, double b) { return (a < b) ? b : a; }  // std::max
 inline double smin(double a, double b) { return (b < a) ? b : a; }  // std::min
@@ -69,7 +69,7 @@ void sph_bisect(const double *a, const double *b, double *c) {
   for (int k = 0; k < 3; ++k) c[k] = r * c[k] / d;
 }
 
-// C = A B with accumulation from zero in index order (matrix.hh:139-155).
+// C = A B with accumulation from zero in index order (mpasoflecsi/eqns/matrix.hh:28-43).
 template <int RA, int CA, int CB>
 void mm(int ra, int ca, int cb, const double (&A)[RA][CA], const double (&B)[CA][CB], double (&C)[RA][CB]) {
   for (int r = 0; r < ra; ++r)
@@ -81,7 +81,7 @@ void mm(int ra, int ca, int cb, const double (&A)[RA][CA], const double (&B)[CA]
 }
 
 // Inverse of a (n x n) by scaled partial-pivoting elimination
-// (matrix.hh:164-279: elgs + migs, T. Pang's method).
+// (matrix.hh:52-167: elgs + migs, T. Pang's method).
 void invert(int n, double (&a)[kNA][kNA], double (&x)[kNA][kNA]) {
   int idx[kNA];
   double scale[kNA], b[kNA][kNA];
@@ -221,7 +221,7 @@ void run(const mpaso_fct_setup_in &in, mpaso_fct_setup_out &o) {
           MPASO_ERR_ARG, "missing input array");
   require(!in.on_sphere || (in.zCell && in.zVertex), MPASO_ERR_ARG, "sphere needs z coordinates");
   const Csr c2e{in.c2e_off, in.c2e}, c2c{in.c2c_off, in.c2c}, e2v{in.e2v_off, in.e2v};
-  // cells(e) by transposition of c2e: ascending ids (mpasoflecsi/specialization/mesh.cc:262-270)
+  // cells(e) by transposition of c2e: ascending ids (mpasoflecsi/specialization/mesh.cc:108-116)
   std::vector<int32_t> e2c0(nE, -1), e2c1(nE, -1);
   for (int64_t c = 0; c < nC; ++c)
     for (int64_t j = 0; j < c2e.n(c); ++j) {

@@ -26,8 +26,8 @@ namespace mpaso {
 namespace {
 
 constexpr int kME = 8, kME2 = 16, kNA = 6, kMM = kME + 1;
-constexpr double kA = 6371000.0;           // mpasoflecsi/common/constants.hh:368
-constexpr double kPi = 3.141592653589793;  // constants.hh:369
+constexpr double kA = 6371000.0;           // mpasoflecsi/common/constants.hh:28
+constexpr double kPi = 3.141592653589793;  // constants.hh:29
 
 // error bits set by the kernels (the host setup's require() checks)
 enum : unsigned {
@@ -93,7 +93,7 @@ __device__ bool sph_bisect(const double *a, const double *b, double *c) {
 __device__ __forceinline__ double wrap(double d, double L) { return L > 0 ? d - L * rint(d / L) : d; }
 
 // Rows 3-5 of the inverse of the 6 x 6 normal matrix by scaled partial-
-// pivoting elimination (mpasoflecsi/eqns/matrix.hh:164-279).  The host setup
+// pivoting elimination (mpasoflecsi/eqns/matrix.hh:52-167).  The host setup
 // eliminates all six right-hand columns together and back-substitutes all six
 // rows; every element here sees the same operations in the same order, one
 // column at a time, and back-substitution stops after the three rows the
@@ -157,7 +157,7 @@ __device__ __forceinline__ void unit_pos(const DevIn &in, int64_t c, double p[3]
   p[0] = in.xCell[c] / kA, p[1] = in.yCell[c] / kA, p[2] = in.zCell[c] / kA;
 }
 
-// cells(e) by transposition of c2e, ascending ids (mesh.cc:262-270): the
+// cells(e) by transposition of c2e, ascending ids (mesh.cc:108-116): the
 // smaller and the larger id of the cells that list the edge.
 __global__ void k_edge_cells(DevIn in, int32_t *e2c0, int32_t *e2c1, int32_t *cnt, unsigned *err) {
   const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

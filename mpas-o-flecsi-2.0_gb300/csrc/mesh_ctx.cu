@@ -1,5 +1,5 @@
 // Mesh context: builds the device-resident mesh from the reference's
-// connectivity (mpasoflecsi/specialization/mesh.cc:221-270 semantics),
+// connectivity (mpasoflecsi/specialization/mesh.cc:67-116 semantics),
 // renumbers it along a Hilbert curve, and uploads slot-major arrays to HBM.
 #include <algorithm>
 #include <cmath>
@@ -59,7 +59,7 @@ Crs copy_crs(const int64_t *off, const int32_t *idx, int64_t n, int64_t n_to, co
   return c;
 }
 
-// v2c[c2v[c][v]].push_back(c) -- mpasoflecsi/specialization/mesh.cc:262-270.
+// v2c[c2v[c][v]].push_back(c) -- mpasoflecsi/specialization/mesh.cc:108-116.
 Crs transpose(const Crs &a, int64_t n_to) {
   Crs t;
   t.off.assign(n_to + 1, 0);

@@ -268,7 +268,7 @@ __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
   vertex_diag(m, st, S, L, v, k, i, u_next, h_next);
 }
 
-// Initial diagnostics (apps/sw/run.cc:226-230).
+// Initial diagnostics (apps/sw/run.cc:88-92).
 // NC = 6: the cell loops unrolled for meshes of at most hexagons (as k_sw_final's unrolled variant)
 template <int NC>
 __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int L) {

@@ -7,9 +7,9 @@ connectivity the way the reference's reader and mesh specialization do:
 - 1-based -> 0-based and zero slots dropped into CRS
   (mpasoflecsi/specialization/definition.hh:693-718);
 - c2v, c2e, c2c, e2v, e2e kept in file order
-  (mpasoflecsi/specialization/mesh.cc:93-105, 224-243);
+  (mpasoflecsi/specialization/mesh.cc:67-89, 93-105);
 - v2c, e2c, v2e built by transposition, i.e. ascending ids
-  (mpasoflecsi/specialization/mesh.cc:262-270).
+  (mpasoflecsi/specialization/mesh.cc:108-116).
 """
 import ctypes
 
@@ -17,8 +17,8 @@ import numpy as np
 
 from ._lib import check, lib
 
-EARTH_RADIUS = 6371000.0  # mpasoflecsi/common/constants.hh:368
-OMEGA = 7.29212e-5  # mpasoflecsi/common/constants.hh:372-373
+EARTH_RADIUS = 6371000.0  # mpasoflecsi/common/constants.hh:28
+OMEGA = 7.29212e-5  # mpasoflecsi/common/constants.hh:32-33
 
 MAX_EDGES = 8
 MAX_EDGES2 = 16

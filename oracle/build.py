@@ -22,7 +22,7 @@ REF_SOURCES = ["apps/sw/tasks/solve.cc", "apps/ocean/tasks/solve.cc",
                "apps/ocean/tasks/init_functions.cc"]
 # (levels, tracers) of the reference builds used by the pin tests.
 REF_CONFIGS = [(1, 1), (3, 2), (5, 5)]
-GRAVITY = "9.80616"  # mpasoflecsi/common/constants.hh:370-371
+GRAVITY = "9.80616"  # mpasoflecsi/common/constants.hh:30-31
 
 
 def _run(cmd):

@@ -470,7 +470,7 @@ static int arc_bisect(double ax, double ay, double az, double bx, double by, dou
 #define MMAX 9 /* at most maxEdges + 1 points */
 
 /* C[r][c] = sum_inner A[r][inner] * B[inner][c], accumulated from 0 in order
- * (mpasoflecsi/eqns/matrix.hh:139-155). */
+ * (mpasoflecsi/eqns/matrix.hh:28-43). */
 static void matmul(int ra, int ca, const double *A, int cb, const double *B, double *C) {
   for (int r = 0; r < ra; ++r)
     for (int col = 0; col < cb; ++col) {
@@ -480,7 +480,7 @@ static void matmul(int ra, int ca, const double *A, int cb, const double *B, dou
     }
 }
 
-/* Partial-pivoting Gaussian elimination (mpasoflecsi/eqns/matrix.hh:164-217). */
+/* Partial-pivoting Gaussian elimination (mpasoflecsi/eqns/matrix.hh:52-105). */
 static void elgs(int n, double *a, int *idx) {
   double cs[NA];
   for (int i = 0; i < n; ++i) idx[i] = i;
@@ -510,7 +510,7 @@ static void elgs(int n, double *a, int *idx) {
   }
 }
 
-/* Matrix inverse via elgs (mpasoflecsi/eqns/matrix.hh:237-279). */
+/* Matrix inverse via elgs (mpasoflecsi/eqns/matrix.hh:125-167). */
 static void migs(int n, double *a, double *x) {
   double b[NA * NA];
   int idx[NA];
@@ -535,7 +535,7 @@ static void migs(int n, double *a, double *x) {
 /* apps/ocean/tasks/init_functions.cc:83-328 (sphere branch; the reference
  * hard-codes on_a_sphere = true at :144). */
 static int init_2nd_deriv(const orc_mesh *m, const orc_geom *g, double *derivTwo) {
-  const double a = 6371000.0, pi = 3.141592653589793; /* constants.hh:368-369 */
+  const double a = 6371000.0, pi = 3.141592653589793; /* constants.hh:28-29 */
   for (int64_t i = 0; i < m->nE * MAXE2 * 2; ++i) derivTwo[i] = 0.0;
   const int64_t nCells = m->nC;
   for (int64_t ic = 0; ic < m->nC; ++ic) {
@@ -873,7 +873,7 @@ int orc_sw_run(const orc_mesh *m, const orc_static *s, const orc_config *c, doub
   memcpy(S.h[PREV], h, sizeof(double) * (size_t)(m->nC * L));
   memcpy(S.u[PREV], u, sizeof(double) * (size_t)(m->nE * L));
   memcpy(S.tr[PREV], tracers, sizeof(double) * (size_t)(m->nC * L * T));
-  sw_diag(m, s, c, &S, PREV); /* apps/sw/run.cc:226-230 */
+  sw_diag(m, s, c, &S, PREV); /* apps/sw/run.cc:88-92 */
   int rc = 0;
   for (int32_t i = 0; i < nsteps && rc == 0; ++i) rc = sw_advance(m, s, c, &S, dt);
   memcpy(h, S.h[PREV], sizeof(double) * (size_t)(m->nC * L));

@@ -28,7 +28,7 @@ extern "C" {
 
 /* Connectivity as the reference's mesh specialization holds it (0-based CRS):
  * file order for c2v, c2e, c2c, e2v, e2e; transposition (ascending ids) for
- * v2c, e2c, v2e (mpasoflecsi/specialization/mesh.cc:221-270). */
+ * v2c, e2c, v2e (mpasoflecsi/specialization/mesh.cc:67-116). */
 enum { ORC_C2V, ORC_C2E, ORC_C2C, ORC_E2V, ORC_E2E, ORC_V2C, ORC_E2C, ORC_V2E, ORC_NCNX };
 typedef struct {
   int64_t nC, nE, nV;
@@ -41,7 +41,7 @@ typedef struct {
   const double *areaCell, *dvEdge, *dcEdge, *areaTriangle, *kiteAreasOnVertex, *fVertex;
   const double *weightsOnEdge; /* me2tensor */
   const double *bottomDepth;   /* h_s of the sw app */
-  /* FCT / del2 statics (apps/ocean/state.hh:261-294) */
+  /* FCT / del2 statics (apps/ocean/state.hh:68-101) */
   const int32_t *maxLevelCell, *maxLevelEdgeTop, *nAdvCellsForEdge;
   const int32_t *advCellsForEdge;  /* me2tensor<int> */
   const int32_t *highOrderAdvMask; /* vltensor<int> */
@@ -130,7 +130,7 @@ int orc_init_layer_thickness_edge(const orc_mesh *m, const orc_config *c, const 
                                   const int32_t *maxLevelEdgeTop, double *hEdge);
 
 /* ---- composed drivers ---- */
-/* sw: apps/sw/run.cc:13-70 (+ the initial diagnostics of run.cc:226-230).
+/* sw: apps/sw/run.cc:13-70 (+ the initial diagnostics of apps/sw/run.cc:88-92).
  * With fct=1 the tracer tendency is the ocean FCT sequence of
  * apps/ocean/run.cc:19-42 applied to the provisional sw state (layer thickness
  * = h[provis], layer thickness at edges = h_edge[provis], velocity = u[provis],

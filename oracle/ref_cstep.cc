@@ -141,7 +141,7 @@ int orc_cstep_sw_run(const orc_mesh *m, const orc_static *s, double dt, int32_t 
       for (std::size_t k = 0; k < L; ++k) S.h[Sw::prev][c][k] = cd(h[c * L + k], eps * dh[c * L + k]);
     for (std::size_t e = 0; e < mv.nE; ++e)
       for (std::size_t k = 0; k < L; ++k) S.u[Sw::prev][e][k] = cd(u[e * L + k], eps * du[e * L + k]);
-    diag(mv, s, S, Sw::prev);  // apps/sw/run.cc:226-230
+    diag(mv, s, S, Sw::prev);  // apps/sw/run.cc:88-92
     for (int i = 0; i < nsteps; ++i) advance(mv, s, S, dt);
     for (std::size_t c = 0; c < mv.nC; ++c)
       for (std::size_t k = 0; k < L; ++k) {

@@ -398,7 +398,7 @@ int orc_init_fct_statics(const orc_mesh *m, const orc_config *c, const orc_geom 
   return guard([&] {
     check_cfg(c);
     auto mv = view_of(m);
-    // apps/ocean/initialize.cc:391-400 (layerThicknessEdge is separate)
+    // apps/ocean/initialize.cc:88-102 (layerThicknessEdge is separate)
     ocean::task::init_maxLevelEdgeTop(mv, F<int>(g->maxLevelCell), F<int>(o->maxLevelEdgeTop));
     ocean::task::init_meshScalingDel2(mv, F<D>(g->meshDensity), F<D>(o->meshScalingDel2));
     ocean::task::init_edgeSignOnCell(mv, F<metensor<D>>(o->edgeSignOnCell));
@@ -434,7 +434,7 @@ int orc_sw_run(const orc_mesh *m, const orc_static *s, const orc_config *c, doub
     std::memcpy(S.h[Sw::prev].data(), h, mv.nC * sizeof(vlreal));
     std::memcpy(S.u[Sw::prev].data(), u, mv.nE * sizeof(vlreal));
     std::memcpy(S.tr[Sw::prev].data(), tracers, mv.nC * sizeof(vltracer));
-    sw_diag(mv, s, S, Sw::prev);  // apps/sw/run.cc:226-230
+    sw_diag(mv, s, S, Sw::prev);  // apps/sw/run.cc:88-92
     for (int i = 0; i < nsteps; ++i) sw_advance(mv, m, s, c, S, dt);
     std::memcpy(h, S.h[Sw::prev].data(), mv.nC * sizeof(vlreal));
     std::memcpy(u, S.u[Sw::prev].data(), mv.nE * sizeof(vlreal));

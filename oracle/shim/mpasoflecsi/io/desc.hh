@@ -1,5 +1,5 @@
 // Oracle shim (test infrastructure only): the output-field descriptors named by
-// apps/sw/state.hh:319-323; the HDF5 machinery behind them is not needed.
+// apps/sw/state.hh:66-70; the HDF5 machinery behind them is not needed.
 #pragma once
 #include "mpasoflecsi/common/types.hh"
 

@@ -2,7 +2,7 @@
 // the reference's tasks use (mpasoflecsi/specialization/mesh.hh:20-75), over
 // CRS connectivity supplied by the oracle driver.  The driver builds c2v, c2e,
 // c2c, e2v, e2e in file order and v2c, e2c, v2e by transposition, as
-// mpasoflecsi/specialization/mesh.cc:221-270 does.
+// mpasoflecsi/specialization/mesh.cc:67-116 does.
 #pragma once
 #include <cstddef>
 #include <cstdint>

@@ -128,6 +128,49 @@ def test_ocean_fct_sequence_bit_exact(case):
     assert np.all(tp <= tmx + 1e-12 * (1 + span)) and np.all(tp >= tmn - 1e-12 * (1 + span))
 
 
+def test_sw_accumulate_and_finalize_bit_exact(case):
+    """accumulate_update (apps/sw/tasks/solve.cc:317-341) and finalize_timestep
+    (solve.cc:344-367) through the C ABI, with and without the pinned wind of
+    test case 1."""
+    g, dm, S, data = case
+    L, T = g.L, g.T
+    om = S.mesh(g.mesh)
+    rng = np.random.default_rng(11)
+    ut, ht, tt = (rng.standard_normal(data["u"].shape), rng.standard_normal(data["h"].shape),
+                  rng.standard_normal(data["tr"].shape))
+    a = [data["u"].copy(), data["h"].copy(), data["h"][..., None] * data["tr"]]
+    b = [x.copy() for x in a]
+    dm.call("sw_accumulate_update", L, T, a[0], ut, a[1], ht, a[2], tt, 12.5)
+    S.call("sw_accumulate_update", om, S.config(L, T), b[0], ut, b[1], ht, b[2], tt, 12.5)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    u_old = rng.standard_normal(data["u"].shape)
+    for pin in (0, 1):
+        ga, gb = [x.copy() for x in a], [x.copy() for x in a]
+        dm.call("sw_finalize_timestep", L, T, u_old, ga[0], ga[1], ga[2], pin)
+        S.call("sw_finalize_timestep", om, S.config(L, T, pin_u=bool(pin)), u_old, gb[0], gb[1], gb[2])
+        for x, y in zip(ga, gb):
+            assert np.array_equal(x, y), pin
+        assert np.array_equal(ga[0], u_old if pin else a[0])
+
+
+def test_ocean_step_tracers_forward_bit_exact(case):
+    """step_tracers_forward (apps/ocean/tasks/solve.cc:368-399) through the C
+    ABI: tracersNew += w tend; tracersPrev = tracers + w_sub tend."""
+    g, dm, S, data = case
+    L, T = g.L, g.T
+    om = S.mesh(g.mesh)
+    rng = np.random.default_rng(13)
+    tend = rng.standard_normal(data["tr"].shape) * 1e-4
+    for w, wsub in ((100.0, 300.0), (50.0, 0.0)):
+        new_a, prev_a = rng.random(data["tr"].shape), np.zeros_like(data["tr"])
+        new_b, prev_b = new_a.copy(), prev_a.copy()
+        dm.call("oc_step_tracers_forward", L, T, tend, data["tr"], new_a, prev_a, w, wsub)
+        S.call("oc_step_tracers_forward", om, S.config(L, T), tend, data["tr"], new_b, prev_b, w, wsub)
+        assert np.array_equal(new_a, new_b)
+        assert np.array_equal(prev_a, prev_b)
+
+
 def test_device_pointers_match_host(case):
     torch = pytest.importorskip("torch")
     g, dm, S, data = case
