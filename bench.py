@@ -38,7 +38,7 @@ for _p in (PKG,):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "SW RK4 cell-updates/s on 1 GB300 & % HBM roofline"
+METRIC = "SW RK4 cell-updates/s on 1 GB300 & % HBM roofline; adjoint/forward time ratio"
 CONFIGS = {
     "sw_l7": dict(workload="sphere-level7 shallow-water RK4 + FCT tracer + del2 (163842 cells, L=1, T=1)",
                   level=7, app="sw", L=1, T=1, dt=60.0, fct=True, hmix=True, kappa=1e4, nu=1e4),
@@ -65,13 +65,13 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def build_workload(cfg, seed):
+def build_workload(cfg, seed, fct=True):
     import mpaso
     from mpaso.initial import ocean_state, sw_state
     from mpaso.setup import fct_statics
     t0 = time.time()
     mesh = mpaso.Mesh.icosa(cfg["level"])
-    fct = fct_statics(mesh, cfg["L"])
+    fct = fct_statics(mesh, cfg["L"]) if fct else None
     if cfg["app"] == "sw":
         state = sw_state(mesh, seed, cfg["L"], cfg["T"])
     else:
@@ -84,7 +84,7 @@ class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, index):
         self.index = index
@@ -102,15 +102,20 @@ class ClockSampler:
         self.p.terminate()
         self.p.wait()
         self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        rows = [[x.strip() for x in r.split(",")] for r in self.f.read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
-        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        num = lambda x: x.replace(".", "", 1).isdigit()  # noqa: E731
+        rows = [r for r in rows if len(r) >= 10 and num(r[1]) and num(r[2])]
+        busy = [r for r in rows if num(r[9]) and float(r[9]) >= 50]
+        under = busy or rows
+        sm = [float(r[1]) for r in under]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4)
-                          if r[5 + i].strip().lower() == "active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(rows), "reasons": reasons}
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(float(r[2]) for r in rows) if rows else None,
+                "samples": len(rows), "samples_under_load": len(busy),
+                "power_w_max": max((float(r[3]) for r in rows if num(r[3])), default=None),
+                "reasons": reasons}
 
 
 def dist_setup():
@@ -120,17 +125,51 @@ def dist_setup():
     return world, rank, local
 
 
-def gpu_arm(args, cfg):
+def workload_config(args, cfg, mesh, world):
+    """The `config` object of the line: what the workload is (the reference
+    arm repeats it verbatim)."""
+    return {"workload": cfg["workload"], "config": args.config, "cells": mesh.nCells, "edges": mesh.nEdges,
+            "vertices": mesh.nVertices, "levels": cfg["L"], "tracers": cfg["T"], "dt_s": cfg["dt"],
+            "fct": cfg["fct"], "del2_tracer": cfg["kappa"], "del2_momentum": cfg["nu"],
+            "parallelism": f"replicas x{world}"}
+
+
+def timed_regions(fn, ext, barrier, min_ms, min_reps=3):
+    """Runs fn() (the timed region) repeatedly, each time bracketed by a
+    barrier and device synchronisation and timed with CUDA events on the
+    state stream, until at least min_ms of regions and min_reps regions ran.
+    The repeat count is fixed before the first timed region (from one
+    untimed calibration region, max over ranks) so every rank runs the same
+    number.  Returns the per-region times in ms."""
+    import torch
+
+    from mpaso.replicas import reduce_over_ranks
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def one():
+        barrier()
+        e0.record(ext)
+        fn()
+        e1.record(ext)
+        e1.synchronize()
+        barrier()
+        return e0.elapsed_time(e1)
+    cal = reduce_over_ranks(one(), "max", device="cuda")
+    reps = max(min_reps, int(-(-min_ms // max(cal, 1e-3))))
+    return [one() for _ in range(reps)]
+
+
+def gpu_arm(args, cfg, extras=True):
     import numpy as np
     import torch
 
     import mpaso.gpu as G
-    from mpaso.perfmodel import Dims, ocean_kernels, per_step, sw_kernels
+    from mpaso.perfmodel import Dims, dataflow_bytes, ocean_kernels, per_step, sw_kernels
     from mpaso.replicas import reduce_over_ranks
 
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
-    if world > 1:
+    if world > 1 and not torch.distributed.is_initialized():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     mesh, fct, state = build_workload(cfg, seed=1000 + rank)
@@ -159,58 +198,77 @@ def gpu_arm(args, cfg):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    # ---- timed region: K graph-replayed steps, repeated for >= min_timed_s
     sampler = ClockSampler(local)
     time.sleep(0.3)
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(ext)
-    st.step_graph(dt, K)
-    e1.record(ext)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    barrier()
+    regions = timed_regions(lambda: st.step_graph(dt, K), ext, barrier, args.min_timed_s * 1e3)
     clocks = sampler.stop()
+    ms = statistics.median(regions)
     ms_max = reduce_over_ranks(ms, "max", device="cuda")
     units_rank = mesh.nCells * cfg["L"]
     value = world * units_rank * K / (ms_max * 1e-3)
+    ms_step = ms_max / K
 
-    # ---- per-kernel timing (live, CUDA events between launches) and roofline
-    prof = st.profile(dt, min(K, 20))
+    # ---- per-kernel device time: shares from the replayed step graph with an
+    # event node after every kernel (the nodes cost the launches their overlap,
+    # so those intervals add up to more than the plain step), applied to the
+    # measured step time so the kernels add up to it
+    prof_raw = st.profile(dt, min(max(K, 10), 50))
+    prof_sum = sum(prof_raw.values())
+    prof = {k: v / prof_sum * ms_step / 4 for k, v in prof_raw.items()}
     dims = Dims.of(mesh, cfg["L"], cfg["T"], fct)
     model = (sw_kernels(dims, cfg["fct"], cfg["hmix"], cfg["nu"] != 0.0) if app == G.APP_SW
              else ocean_kernels(dims, cfg["fct"], cfg["hmix"]))
-    step_bytes, step_fp64 = per_step(model)
-    top = max(prof, key=prof.get)
-    prof_total = sum(prof.values())
+    model_bytes, step_fp64 = per_step(model)
+    prof_step = 4 * prof_sum
     peak, peak_kind = measured_peaks()
-    kb, kf = model[top]
-    achieved = kb / (prof[top] * 1e-3) / 1e9
+    # roofline of record: the whole step's minimal-dataflow bytes over the
+    # step time; the step is the unit the bytes are defined on (each array
+    # once per stage, summed over the fused kernels)
+    step_bytes = dataflow_bytes(mesh, cfg["L"], cfg["T"], fct, cfg["fct"], cfg["hmix"])
+    achieved = step_bytes / (ms_step * 1e-3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", f"{top}_{args.config}.txt")
-    if os.path.exists(tfile):
-        for line in open(tfile):
-            if line.startswith("dram_bytes_per_launch:"):
-                traffic = float(line.split(":")[1])
+    tkern = {}
+    for k in model:
+        tfile = os.path.join(ROOT, "profiles", f"{k}_{args.config}.txt")
+        if os.path.exists(tfile):
+            for line in open(tfile):
+                if line.startswith("dram_bytes_per_launch:"):
+                    tkern[k] = float(line.split(":")[1])
+    if len(tkern) == len(model):
+        traffic = 4 * sum(tkern.values())
+    top = max(prof, key=prof.get)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": top,
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "kernel": "rk4_step (the graph of 3 kernels x 4 RK stages)",
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s",
-                "algorithmic_bytes_per_launch": int(kb),
-                "kernel_time_share": round(prof[top] / prof_total, 3)}
-    # FP64 pipe peak: 2 DFMA/DADD/DMUL per clock per SM (ncu's peak for the pipe; the
-    # ocean edge kernel sustains 91% of it).  A chain of dependent DFMAs alone (the
-    # probe) issues at ~0.80 of it.
-    pipe_peak = 2.0 * torch.cuda.get_device_properties(local).multi_processor_count * \
-        (clocks.get("sm_max_mhz") or 2070.0) * 1e6
-    fp64 = {"achieved_per_s": kf / (prof[top] * 1e-3), "peak_per_s": pipe_peak,
-            "frac": round(kf / (prof[top] * 1e-3) / pipe_peak, 4), "kernel": top,
-            "step_frac": round(step_fp64 / (ms_max * 1e-3 / K) / pipe_peak, 4),
-            "note": "FP64 instructions per launch from mpaso/perfmodel.py (within ~10% of ncu's counts) "
-                    "/ measured launch time, against the FP64 pipe peak of 2 per clock per SM"}
-    step_hbm = {"algorithmic_bytes_per_step": int(step_bytes),
-                "achieved_gbs": round(step_bytes / (ms_max * 1e-3 / K) / 1e9, 1),
-                "frac": round(step_bytes / (ms_max * 1e-3 / K) / 1e9 / peak, 4),
-                "bytes_per_cell_update": round(step_bytes / units_rank, 1)}
+                "byte_model": "minimal fused dataflow: each array read/written once per RK stage "
+                              "(mpaso/perfmodel.py dataflow_bytes)",
+                "algorithmic_bytes_per_step": int(step_bytes),
+                "bytes_per_cell_update": round(step_bytes / units_rank, 1),
+                "traffic_note": "sum over the step's 12 launches of ncu dram__bytes_read + write (profiles/)",
+                "traffic_model": {"per_launch_bytes_per_step": int(model_bytes),
+                                  "frac": round(model_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
+                                  "note": "every array each launch touches, re-reads across the three "
+                                          "kernels of a stage included (mpaso/perfmodel.py sw_kernels)"},
+                "dominant_kernel": top, "dominant_kernel_time_share": round(prof[top] / sum(prof.values()), 3)}
+    # FP64 pipe: 2 DFMA/DADD/DMUL per clock per SM (ncu's peak for the pipe),
+    # at the median SM clock under load
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    pipe_peak = 2.0 * sms * mhz * 1e6
+    fp64 = {"bound": "fp64", "peak_per_s": pipe_peak,
+            "peak_note": f"2 FP64 instructions per clock per SM x {sms} SMs x {mhz:.0f} MHz (median under load)",
+            "step_frac": round(step_fp64 / (ms_step * 1e-3) / pipe_peak, 4),
+            "instructions_per_cell_update": round(step_fp64 / units_rank, 1),
+            "per_kernel_frac": {k: round(model[k][1] / (prof[k] * 1e-3) / pipe_peak, 4) for k in model},
+            "note": "FP64 thread instructions from mpaso/perfmodel.py (within ~10% of ncu's counts) over the "
+                    "graph-replayed time; the FP64 pipe, not HBM, is the binding ceiling of this path"}
+    kernels = {k: {"ms_per_launch": round(v, 5), "share": round(v / sum(prof.values()), 3),
+                   "model_bytes": int(model[k][0]),
+                   "model_gbs": round(model[k][0] / (v * 1e-3) / 1e9, 1),
+                   "ncu_dram_bytes": tkern.get(k)} for k, v in prof.items()}
 
     # ---- end to end through the C ABI with host buffers (pinned)
     Ke = min(K, 200)
@@ -220,43 +278,39 @@ def gpu_arm(args, cfg):
         nbytes = (hp.numel() + up.numel() + tp.numel()) * 8
         st.step_host(dt, 1, hp, up, tp)  # warm the staging path
         torch.cuda.synchronize()
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(ext)
-        for _ in range(Ke):
-            st.step_host(dt, 1, hp, up, tp)
-        a1.record(ext)
-        a1.synchronize()
-        blocking_ms = a0.elapsed_time(a1)
-        # the same calls queued (mpaso_rk4_step_host_async): each still copies its
-        # inputs in from and its results out to the page-locked buffers, in order,
-        # but the host does not wait in between; one sync at the end
+
+        def blocking():
+            for _ in range(Ke):
+                st.step_host(dt, 1, hp, up, tp)
+
+        def queued():
+            # each call still copies its inputs in from and its results out to
+            # the page-locked buffers, in order, but the host does not wait in
+            # between; one sync at the end
+            for _ in range(Ke):
+                st.step_host_async(dt, 1, hp, up, tp)
+            st.sync()
         st.step_host_async(dt, 1, hp, up, tp)
         st.sync()
-        a0.record(ext)
-        for _ in range(Ke):
-            st.step_host_async(dt, 1, hp, up, tp)
-        a1.record(ext)
-        st.sync()
-        a1.synchronize()
-        e2e_ms = a0.elapsed_time(a1)
+        blocking_ms = statistics.median(timed_regions(blocking, ext, barrier, args.min_timed_s * 5e2))
+        e2e_ms = statistics.median(timed_regions(queued, ext, barrier, args.min_timed_s * 5e2))
     else:
         tp = pin(tr)
         nbytes = tp.numel() * 8
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(ext)
-        for _ in range(Ke):
-            st.set(G.FIELD_TRACERS, tp)
-            st.step_graph(dt, 1)
-            st.get(G.FIELD_TRACERS, tp.numpy())
-        a1.record(ext)
-        a1.synchronize()
-        e2e_ms = a0.elapsed_time(a1)
+
+        def io_steps():
+            for _ in range(Ke):
+                st.set(G.FIELD_TRACERS, tp)
+                st.step_graph(dt, 1)
+                st.get(G.FIELD_TRACERS, tp.numpy())
+        e2e_ms = statistics.median(timed_regions(io_steps, ext, barrier, args.min_timed_s * 5e2))
     e2e_max = reduce_over_ranks(e2e_ms, "max", device="cuda")
     e2e = {"value": world * units_rank * Ke / (e2e_max * 1e-3), "unit": "cell-updates/s",
            "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes),
            "path": "mpaso_rk4_step_host_async x steps, then mpaso_state_sync (C ABI, pinned host buffers: "
                    "copy in -> 1 step -> copy out every step)"
-           if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)"}
+           if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)",
+           "timing": f"median of repeated regions of {Ke} calls"}
     if app == G.APP_SW:
         bl = reduce_over_ranks(blocking_ms, "max", device="cuda")
         e2e["blocking"] = {"value": world * units_rank * Ke / (bl * 1e-3),
@@ -290,29 +344,34 @@ def gpu_arm(args, cfg):
 
     out = None
     if rank == 0:
-        cpu = cpu_baseline(cfg, mesh, fct, state) if (world == 1 and not args.no_cpu_baseline) else None
+        cpu = (cpu_baseline(cfg, mesh, fct, state)
+               if (world == 1 and not args.no_cpu_baseline and extras) else None)
         working_set = dm.device_bytes() + st.device_bytes()
         out = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": K,
-            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "warmup": W, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded smooth fields on generated mesh)",
-            "config": {"workload": cfg["workload"], "config": args.config, "cells": mesh.nCells,
-                       "edges": mesh.nEdges, "vertices": mesh.nVertices, "levels": cfg["L"],
-                       "tracers": cfg["T"], "dt_s": dt, "fct": cfg["fct"], "del2_tracer": cfg["kappa"],
-                       "del2_momentum": cfg["nu"], "parallelism": f"replicas x{world}",
-                       "l2": f"device working set {working_set / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2 "
-                             "(no flush)", "timing": "CUDA events on the state stream, graph-replayed steps",
-                       "launch": dict(launch, autotuned=not args.no_autotune)},
-            "roofline": roofline, "fp64": fp64, "step_hbm": step_hbm,
-            "kernels_ms_per_launch": {k: round(v, 5) for k, v in prof.items()},
+            "config": workload_config(args, cfg, mesh, world),
+            "run": {"timing": f"CUDA events on the state stream; the {K}-step graph-replayed region repeated "
+                              f"{len(regions)} times (>= {args.min_timed_s} s), median region reported",
+                    "regions_ms": {"median": round(ms, 4), "min": round(min(regions), 4),
+                                   "max": round(max(regions), 4), "count": len(regions)},
+                    "l2": f"device working set {working_set / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2 "
+                          "(inputs larger than L2, no flush)",
+                    "launch": dict(launch, autotuned=not args.no_autotune),
+                    "profiled_step_ms": round(prof_step, 5),
+                    "kernel_times": "per-kernel shares from the step graph replayed with an event node after "
+                                    "every kernel (that graph's step: profiled_step_ms), times the measured "
+                                    "step; ncu launch-list shares in profiles/"},
+            "roofline": roofline, "fp64": fp64,
+            "kernels_ms_per_launch": {k: round(v, 5) for k, v in prof.items()}, "kernels": kernels,
             "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu, "diagnostics": diagnostics,
             "gpu_launches": st.launches_per_step() * K,
+            "gpu_launches_note": f"per timed region: {st.launches_per_step()} kernels per step x {K} steps "
+                                 f"(the region ran {len(regions)} times)",
         }
     st.close()
     dm.close()
-    if world > 1:
-        torch.distributed.barrier()
-        torch.distributed.destroy_process_group()
     return out
 
 
@@ -718,15 +777,62 @@ def ensemble_arm(args):
 
 
 # ---------------------------------------------------------------- reference arm
-def _ref_worker(args):
-    cfg_name, steps, warmup, seed, kind, barrier = args
-    sys.path.insert(0, PKG)
+_REF_FIELDS = ("areaCell", "dvEdge", "dcEdge", "areaTriangle", "kiteAreasOnVertex", "fVertex", "weightsOnEdge")
+
+
+def make_ref_inputs(cfg_name, seed, path):
+    """Writes the reference arm's inputs -- the mesh's connectivity (as the
+    reference's mesh holds it) and geometry, the FCT statics from the oracle
+    and the seeded initial state -- to `path` (.npz).  Runs in its own
+    process, so the processes that time the reference load nothing but the
+    oracle."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
     from oracle import Oracle
     cfg = CONFIGS[cfg_name]
-    mesh, _, state = build_workload(cfg, seed)
-    O = Oracle("restatement") if kind == "port" else Oracle("ref", cfg["L"], cfg["T"])
+    mesh, _, state = build_workload(cfg, seed, fct=False)
+    O = Oracle("restatement")
     fct = O.fct_statics(mesh, cfg["L"], cfg=O.config(cfg["L"], cfg["T"]))
+    arrays = {f"f_{k}": mesh.fields[k] for k in _REF_FIELDS}
+    arrays.update({f"fct_{k}": v for k, v in fct.items()})
+    for name, (off, idx) in mesh.crs().items():
+        arrays[f"off_{name}"], arrays[f"idx_{name}"] = off, idx
+    arrays.update({f"state_{i}": a for i, a in enumerate(state)})
+    arrays["sizes"] = np.array([mesh.nCells, mesh.nEdges, mesh.nVertices, len(state)], np.int64)
+    np.savez(path, **arrays)
+
+
+class MeshSizes:
+    def __init__(self, nC, nE, nV):
+        self.nCells, self.nEdges, self.nVertices = nC, nE, nV
+
+
+class SavedMesh:
+    """The mesh as the oracle reads it (sizes, fields, reference-ordered CRS),
+    loaded from make_ref_inputs' file."""
+
+    def __init__(self, z):
+        self.nCells, self.nEdges, self.nVertices = (int(x) for x in z["sizes"][:3])
+        self.fields = {k: z[f"f_{k}"] for k in _REF_FIELDS}
+        self._crs = {k[4:]: (z[k], z["idx_" + k[4:]]) for k in z.files if k.startswith("off_")}
+
+    def crs(self):
+        return self._crs
+
+
+def _ref_load(cfg_name, inputs, kind):
+    """(units, run(n)) of the reference arm in this process, from the inputs file."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    from oracle import Oracle
+    cfg = CONFIGS[cfg_name]
+    z = np.load(inputs)
+    mesh = SavedMesh(z)
+    fct = {k[4:]: z[k] for k in z.files if k.startswith("fct_")}
+    state = [z[f"state_{i}"] for i in range(int(z["sizes"][3]))]
+    O = Oracle("restatement") if kind == "port" else Oracle("ref", cfg["L"], cfg["T"])
     st, om = O.static(mesh, fct), O.mesh(mesh)
     c = O.config(cfg["L"], cfg["T"], fct=cfg["fct"], hmix=cfg["hmix"], kappa=cfg["kappa"], nu=cfg["nu"])
 
@@ -734,15 +840,36 @@ def _ref_worker(args):
         if cfg["app"] == "sw":
             return O.sw_run(om, st, c, cfg["dt"], n, *state)
         return O.ocean_run(om, st, c, cfg["dt"], n, *state)
-    if warmup:
-        run(warmup)
+    return mesh, run
+
+
+def _ref_size(args):
+    """Seconds of one step of the reference arm (one core)."""
+    cfg_name, inputs, kind = args
+    mesh, run = _ref_load(cfg_name, inputs, kind)
+    t0 = time.perf_counter()
+    run(1)
+    return time.perf_counter() - t0, (mesh.nCells, mesh.nEdges, mesh.nVertices)
+
+
+def _ref_timed(args):
+    cfg_name, inputs, kind, steps, warm, barrier = args
+    mesh, run = _ref_load(cfg_name, inputs, kind)
+    if warm:
+        run(warm)  # untimed warm-up in this process
     barrier.wait()  # every process built and warmed up; the parent starts its clock
     t0 = time.perf_counter()
     run(steps)
-    return mesh.nCells * cfg["L"], time.perf_counter() - t0
+    return mesh.nCells * CONFIGS[cfg_name]["L"], time.perf_counter() - t0
 
 
 def reference_arm(args, cfg):
+    """The reference algorithm on the host cores: the shim-built reference
+    task sources where they were built, else the oracle's C restatement
+    (bit-identical to them), one process per core, each advancing its own copy
+    of the workload.  Inputs are made once in a separate process; the timed
+    processes load only the oracle library.  Steps per process: --steps when
+    the CPU budget allows it, else as many as fit (the line says which)."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return None
@@ -756,34 +883,102 @@ def reference_arm(args, cfg):
             kind = "reference"
         except OSError:
             kind = "port"
-    steps = max(1, min(args.steps, args.ref_max_steps))
-    warm = min(args.warmup, 3)  # untimed warm-up steps per process (~0.4 s each at level 7)
     cores = args.ref_procs or (os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
-    mgr = ctx.Manager()
-    barrier = mgr.Barrier(cores + 1)
-    with ctx.Pool(cores) as pool:
-        res = pool.map_async(_ref_worker, [(args.config, steps, warm, 2000 + i, kind, barrier)
-                                           for i in range(cores)])
-        barrier.wait()
-        t0 = time.perf_counter()
-        out = res.get()
-        wall = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as tmp:
+        inputs = os.path.join(tmp, "inputs.npz")
+        t0 = time.time()
+        p = ctx.Process(target=make_ref_inputs, args=(args.config, 2000, inputs))
+        p.start()
+        p.join()
+        if p.exitcode != 0:
+            raise RuntimeError("reference arm: making the inputs failed")
+        log(f"reference inputs made in {time.time() - t0:.1f}s")
+        # one process sizes the sample: a step's CPU time against the budget
+        with ctx.Pool(1) as pool:
+            t1, sizes = pool.apply(_ref_size, ((args.config, inputs, kind),))
+        warm = max(1, min(args.warmup, int(0.1 * args.ref_budget_s / t1)))
+        steps = max(1, min(args.steps, int((args.ref_budget_s - warm * t1) / t1)))
+        barrier = ctx.Manager().Barrier(cores + 1)
+        with ctx.Pool(cores) as pool:
+            res = pool.map_async(_ref_timed, [(args.config, inputs, kind, steps, warm, barrier)
+                                              for _ in range(cores)])
+            barrier.wait()
+            t0 = time.perf_counter()
+            out = res.get()
+            wall = time.perf_counter() - t0
     units = [u for u, _ in out]
     times = [t for _, t in out]
     value = sum(units) * steps / max(max(times), 1e-9)
-    desc = (f"{cores} processes x {steps} RK4 steps of the {cfg['workload']} workload, "
-            f"{'reference task sources via the oracle shim' if kind == 'reference' else 'oracle C restatement of the reference tasks'}, "
-            "gcc -O3, one thread each")
-    return {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": steps,
+    desc = (f"{cores} processes x {steps} RK4 steps of the {cfg['workload']} workload (each process its own "
+            f"copy), {'reference task sources via the oracle shim' if kind == 'reference' else 'oracle C restatement of the reference tasks'}, "
+            "gcc -O3, one thread each; inputs (mesh, FCT statics, initial state) made beforehand in a "
+            "separate process")
+    line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": steps,
             "warmup": warm, "ms_per_step": max(times) / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded smooth fields on generated mesh)", "impl": "reference",
-            "config": {"workload": cfg["workload"], "config": args.config, "wall_s": round(wall, 2)},
+            "config": workload_config(args, cfg, MeshSizes(*sizes), world),
+            "run": {"wall_s": round(wall, 2), "first_step_s": round(t1, 3), "cpu_budget_s": args.ref_budget_s},
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": kind,
                              "sample": desc},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
+    if steps < args.steps:
+        line["run"]["steps_note"] = (f"{steps} of the requested {args.steps} steps per process: a step takes "
+                                     f"{t1:.2f} s of one core, and the sample is held to {args.ref_budget_s:.0f} s")
+    if warm < args.warmup:
+        line["run"]["warmup_note"] = f"{warm} untimed warm-up steps (of {args.warmup}) within the budget"
+    return line
+
+
+def extras_for_line(args):
+    """The rest of the metric, measured in the same run: the adjoint (level-6
+    sphere, 500 steps, checkpoints every 25), the 60-level ocean workload and
+    the 256-member ensemble, each summarised.  A part that fails records its
+    error instead of stopping the line."""
+    out = {}
+    t0 = time.time()
+    try:
+        a = adjoint_arm(args)
+        tr, oc = a.get("tracers") or {}, a.get("ocean_tracers") or {}
+        out["adjoint"] = {
+            "workload": a["config"]["workload"], "vjp_over_forward": a["value"],
+            "gradient_over_plain_forward": (a["forward_ms"] + a["vjp_ms"]) / a["forward_plain_ms"],
+            "forward_ms": a["forward_ms"], "forward_plain_ms": a["forward_plain_ms"], "vjp_ms": a["vjp_ms"],
+            "fd_check": a["fd_check"], "peak_device_bytes": a["peak_device_bytes"],
+            "stored_window": a["stored_window"],
+            "with_tracer": {k: tr.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
+                                                   "peak_device_bytes")},
+            "ocean_tracers": {k: oc.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
+                                                     "peak_device_bytes")}}
+    except Exception as e:  # noqa: BLE001
+        out["adjoint"] = {"error": repr(e)}
+    log(f"extras: adjoint done at {time.time() - t0:.0f}s")
+    try:
+        sub = argparse.Namespace(**vars(args))
+        sub.config, sub.steps, sub.no_cpu_baseline = "ocean_l7", min(args.steps, 20), True
+        o = gpu_arm(sub, CONFIGS["ocean_l7"], extras=False)
+        out["cfg2"] = {"workload": o["config"]["workload"], "value": o["value"],
+                       "unit": "cell-level-updates/s", "ms_per_step": o["ms_per_step"], "steps": o["steps"],
+                       "roofline_frac": o["roofline"]["frac"], "roofline": o["roofline"],
+                       "fp64_step_frac": o["fp64"]["step_frac"], "fp64": o["fp64"],
+                       "kernels_ms_per_launch": o["kernels_ms_per_launch"], "e2e": o["e2e"],
+                       "diagnostics": o["diagnostics"], "launch": o["run"]["launch"], "clocks": o["clocks"]}
+    except Exception as e:  # noqa: BLE001
+        out["cfg2"] = {"error": repr(e)}
+    log(f"extras: cfg2 done at {time.time() - t0:.0f}s")
+    try:
+        e = ensemble_arm(args)
+        out["ensemble"] = {k: e[k] for k in ("value", "unit", "steps", "cell_updates_per_s", "one_at_a_time",
+                                             "speedup_vs_one_at_a_time", "one_at_a_time_serial",
+                                             "speedup_vs_serial", "setup")}
+        out["ensemble"]["workload"] = e["config"]["workload"]
+        out["ensemble"]["launch"] = e["config"]["launch"]
+    except Exception as e:  # noqa: BLE001
+        out["ensemble"] = {"error": repr(e)}
+    out["extras_wall_s"] = round(time.time() - t0, 1)
+    return out
 
 
 def main():
@@ -803,7 +998,12 @@ def main():
     ap.add_argument("--ens-levels", default="5,6", help="sphere member levels to draw from")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
-    ap.add_argument("--ref-max-steps", type=int, default=4, help="reference arm: steps timed per process")
+    ap.add_argument("--min-timed-s", type=float, default=1.5,
+                    help="repeat the timed region until this many seconds of it ran (median reported)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only (no adjoint, 60-level ocean and ensemble objects)")
+    ap.add_argument("--ref-budget-s", type=float, default=90.0,
+                    help="reference arm: CPU seconds per process for warm-up + timed steps")
     ap.add_argument("--ref-procs", type=int, default=0, help="reference arm: processes (0 = all cores)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
@@ -820,7 +1020,17 @@ def main():
         out = ensemble_arm(args)
     else:
         cfg = CONFIGS[args.config]
-        out = reference_arm(args, cfg) if args.impl == "reference" else gpu_arm(args, cfg)
+        if args.impl == "reference":
+            out = reference_arm(args, cfg)
+        else:
+            out = gpu_arm(args, cfg)
+            world, rank, _ = dist_setup()
+            if out is not None and world == 1 and args.config == "sw_l7" and not args.no_extras:
+                out.update(extras_for_line(args))
+            if world > 1:
+                import torch
+                torch.distributed.barrier()
+                torch.distributed.destroy_process_group()
     if out is not None:
         print(json.dumps(out), flush=True)
 

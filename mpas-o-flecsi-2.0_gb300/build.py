@@ -27,9 +27,10 @@ CUDA_INC = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(
     shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc"))), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
-# Per-file extra flags: the per-task kernels keep every multiply and add
-# separately rounded so that they reproduce the reference tasks bit for bit.
-FILE_FLAGS = {"tasks.cu": ["-fmad=false"], "fct_setup_dev.cu": ["-fmad=false"]}
+# Per-file extra flags: the per-task kernels and the ocean app's fused stage
+# kernels keep every multiply and add separately rounded so that they
+# reproduce the reference tasks value for value.
+FILE_FLAGS = {"tasks.cu": ["-fmad=false"], "fct_setup_dev.cu": ["-fmad=false"], "ocean.cu": ["-fmad=false"]}
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 

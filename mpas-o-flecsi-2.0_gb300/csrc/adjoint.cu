@@ -139,7 +139,7 @@ struct TrArgs {
   const double *u, *h, *tr;        // stage input (tape)
   const double *A, *LO;            // stage fluxes (tape)
   const double2 *R2;               // stage limiter factors (tape)
-  const double *hpi, *tLO;         // stage 1/hProv and area-weighted upwind sum (tape)
+  const double *hpi, *tLO;         // stage 1/hProv and upwind sum (tape; area-weighted unless ocean)
   const double *kd;                // del2 coefficient per edge
   double *lk_h;                    // thickness-tendency cotangent, + dt lambda_hProv in place
   double *lk_q, *gq, *lam_q, *acc_q;
@@ -412,7 +412,9 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
     }
     fi = lane_sum<NL>(fi), fo = lane_sum<NL>(fo), lrp = lane_sum<NL>(lrp), lrm = lane_sum<NL>(lrm);
     if (lane) continue;
-    const double num = fma(dtia, a.tLO[it], trc * hin);
+    // upwind sum: area-weighted from the sw kernels, divided by the area (as
+    // the reference's tend holds it) from the ocean kernels
+    const double num = fma(a.ocean ? a.dt : dtia, a.tLO[it], trc * hin);
     const double up = num * hpi;
     double lup = 0.0, ldp = 0.0, ldm = 0.0;
     double2 lb = make_double2(0.0, 0.0);  // cotangents of the max / min bounds

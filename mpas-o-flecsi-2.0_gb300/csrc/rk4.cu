@@ -517,7 +517,7 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
   } else {
     launch_k1<T, 0>(s, S, u1, s.tune_tpb[0], st);
   }
-  if (ev) MPASO_CUDA(cudaEventRecord(ev[0], st));
+  if (ev) prof_mark(ev[0], st);
   if (split) {
     if (OC1 && s.tune_occ[1])
       launch_k2<T, OC1, 1>(s, S, u2, s.tune_tpb[1], st);
@@ -528,13 +528,13 @@ template <int T> void launch_stage_T(SwState &s, const Stage &S, cudaStream_t st
   } else {
     launch_k2<T, 0, 0>(s, S, u2, s.tune_tpb[1], st);
   }
-  if (ev) MPASO_CUDA(cudaEventRecord(ev[1], st));
+  if (ev) prof_mark(ev[1], st);
   if (s.k2_mark) MPASO_CUDA(cudaEventRecord(s.k2_mark, st));
   if (OC1 && s.tune_occ[2])
     launch_k3<T, OC1>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
   else
     launch_k3<T, 0>(s, S, c6 && s.tune_unroll[2], s.tune_tpb[2], st);
-  if (ev) MPASO_CUDA(cudaEventRecord(ev[2], st));
+  if (ev) prof_mark(ev[2], st);
 }
 
 void launch_stage(SwState &s, const Stage &S, cudaStream_t st) {
@@ -669,41 +669,63 @@ void run_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
 }
 
 // Device time (ms per launch) of the three stage kernels over nsteps RK4
-// steps, from events recorded between the launches; advances the state.
+// steps; advances the state.  One step is captured as a graph with an event
+// node before the first kernel and after every kernel of each stage, and the
+// graph is replayed nsteps times: the kernels run as the step graph runs them
+// (no host round trip between launches), and the intervals between the event
+// nodes add up to the step.
 void time_stage_kernels(SwState &S, double dt, int nsteps, double ms[3]) {
   const bool oc = S.p.app == MPASO_APP_OCEAN;
-  constexpr int nk = 3;
+  constexpr int nk = 3, nev = 4 * nk + 1;
   if (oc)
     ocean_prepare(S, dt, S.stream);
   else
     ensure_diag(S, S.stream);
-  cudaEvent_t ev[nk + 1] = {};
+  cudaEvent_t ev[nev] = {};
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
   double acc[nk] = {0, 0, 0};
+  auto release = [&] {
+    S.prof_events = nullptr;
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  };
   try {
     for (auto &e : ev) MPASO_CUDA(cudaEventCreate(&e));
-    S.prof_events = ev + 1;
-    for (int n = 0; n < nsteps; ++n)
+    MPASO_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      MPASO_CUDA(cudaEventRecordWithFlags(ev[0], S.stream, cudaEventRecordExternal));
       for (int rk = 0; rk < 4; ++rk) {
-        MPASO_CUDA(cudaEventRecord(ev[0], S.stream));
+        S.prof_events = ev + 1 + nk * rk;
         if (oc)
           ocean_one_stage(S, rk, dt, S.stream);
         else
           launch_stage(S, make_stage(S, rk, dt), S.stream);
-        MPASO_CUDA(cudaEventSynchronize(ev[nk]));
-        for (int k = 0; k < nk; ++k) {
-          float t = 0.f;
-          MPASO_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
-          acc[k] += t;
-        }
       }
+      S.prof_events = nullptr;
+    } catch (...) {
+      cudaStreamEndCapture(S.stream, &g);
+      cudaGetLastError();
+      throw;
+    }
+    MPASO_CUDA(cudaStreamEndCapture(S.stream, &g));
+    MPASO_CUDA(cudaGraphInstantiate(&ge, g, 0));
+    for (int n = 0; n < nsteps; ++n) {
+      MPASO_CUDA(cudaGraphLaunch(ge, S.stream));
+      MPASO_CUDA(cudaEventSynchronize(ev[nev - 1]));
+      for (int j = 0; j < nev - 1; ++j) {
+        float t = 0.f;
+        MPASO_CUDA(cudaEventElapsedTime(&t, ev[j], ev[j + 1]));
+        acc[j % nk] += t;
+      }
+    }
   } catch (...) {
-    S.prof_events = nullptr;
-    for (auto &e : ev)
-      if (e) cudaEventDestroy(e);
+    release();
     throw;
   }
-  S.prof_events = nullptr;
-  for (auto &e : ev) MPASO_CUDA(cudaEventDestroy(e));
+  release();
   for (int k = 0; k < nk; ++k) ms[k] = acc[k] / (4.0 * nsteps);
 }
 

@@ -53,6 +53,12 @@ void launch_pdl(void (*kern)(K...), int64_t n, int threads, bool pdl, cudaStream
   MPASO_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
 }
 
+// Timing mark after a stage kernel (SwState::prof_events): an event node of
+// the step graph being captured for the per-kernel profile.
+inline void prof_mark(cudaEvent_t ev, cudaStream_t st) {
+  MPASO_CUDA(cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal));
+}
+
 // Per-state derived statics (device arrays), built once at state creation.
 // The sw kernels carry the doubled thickness flux F2 = u (h1 + h2) = 2 F and
 // the doubled edge PV Pv = pv_a + pv_b = 2 pv_e; the power-of-two factors are
@@ -149,7 +155,8 @@ struct SwState {
   size_t out_bytes = 0;
   int out_next = 0;
   cudaEvent_t out_ready = nullptr, out_read[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
-  // optional per-launch timing: events recorded after every kernel of a stage
+  // per-launch timing: event nodes recorded after every kernel of a stage
+  // while the profiled step graph is captured (time_stage_kernels)
   cudaEvent_t *prof_events = nullptr;
   // adjoint buffers (checkpoints, stage tape, cotangents); see adjoint.cu
   struct AdjBuffers *adj = nullptr;

@@ -11,6 +11,11 @@ runs on the integer pipe and is not counted.  ncu's counts for the same
 launches are in profiles/ (within about 10% of these).
 
 One cell-update = one cell x one level advanced by one full RK4 step.
+
+Two byte models are kept.  `dataflow_bytes` is the model of record for the
+roofline: the minimal fused dataflow, each array counted once per RK stage.
+`sw_kernels` / `ocean_kernels` count what each launch touches, re-reads across
+the three kernels of a stage included; they explain per-kernel traffic.
 """
 from dataclasses import dataclass
 
@@ -33,6 +38,46 @@ class Dims:
         maxAdv = int(fct_statics["nAdvCellsForEdge"].max()) if fct_statics is not None else 1
         return cls(mesh.nCells, mesh.nEdges, mesh.nVertices, L, T, maxEoE, maxAdv,
                    float(f["nEdgesOnCell"].mean()))
+
+
+def dataflow_bytes(mesh, L, T, fct_statics=None, fct=True, hmix=True):
+    """Algorithmic bytes of one RK4 step in the minimal fused dataflow: every
+    array read or written once per RK stage (FP64 = 8 B, index = 4 B), from
+    the mesh's own sums of the ragged counts.
+
+    Per stage:
+      shallow-water statics -- edges: cellsOnEdge 8, verticesOnEdge 8, dvEdge 8,
+        dcEdge 8, nEdgesOnEdge 4, per edgesOnEdge slot index 4 + weight 8;
+        cells: areaCell 8, bottom depth 8, nEdgesOnCell 4, per edge slot 4
+        (edge signs follow from cellsOnEdge); vertices: cellsOnVertex 12,
+        kites 24, areaTriangle 8, fVertex 8, edgesOnVertex 12;
+      shallow water per level -- h and u: stage input, step start, accumulator
+        read + write, next stage input (5 x 8 B per cell and edge); the
+        compulsory intermediates pv (vertices) and ke (cells), write + read
+        (del2 momentum adds no array: its divergence folds into the cell
+        function ke - nu div that the gradient already reads);
+      FCT + del2 tracer statics -- nAdvCellsForEdge 4 and per stencil slot
+        index 4 + advCoef 8 + advCoef_3rd 8 per edge; cellsOnCell (4 per slot
+        + 4 per cell); meshScalingDel2 8 per edge;
+      per level and tracer -- the tracer state as h and u (5 x 8 per cell),
+        the limiter factors R+ and R- write + read (32 per cell), the
+        anti-diffusive flux write + read (16 per edge).
+    Without tracers the tracer rows drop out."""
+    f = mesh.fields
+    nC, nE, nV = mesh.nCells, mesh.nEdges, mesh.nVertices
+    s_eoe = float(f["nEdgesOnEdge"].sum())
+    s_eoc = float(f["nEdgesOnCell"].sum())
+    stage = 36 * nE + 12 * s_eoe + 20 * nC + 4 * s_eoc + 64 * nV
+    stage += L * (40 * (nC + nE) + 16 * (nV + nC))
+    if T:
+        if fct:
+            s_adv = (float(fct_statics["nAdvCellsForEdge"].sum()) if fct_statics is not None
+                     else 10.0 * nE)
+            stage += 4 * nE + 20 * s_adv + 4 * s_eoc + 4 * nC
+        if hmix:
+            stage += 8 * nE
+        stage += L * T * (40 * nC + (32 * nC + 16 * nE if fct else 0))
+    return 4 * stage
 
 
 def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):

@@ -46,3 +46,40 @@ def have_gpu():
         return device_count() > 0
     except Exception:
         return False
+
+
+def _ocean_slice(args):
+    """Oracle ocean run of one block of levels (a spawned worker)."""
+    import sys
+    level, f, opts, dt, nsteps, h, hE, u, tr, oracle_dir = args
+    if oracle_dir not in sys.path:
+        sys.path.insert(0, oracle_dir)
+    from oracle import Oracle
+    mesh = mpaso.Mesh.icosa(level)
+    S = Oracle("restatement")
+    L, T = h.shape[1], tr.shape[2]
+    return S.ocean_run(mesh, S.static(mesh, f), S.config(L, T, **opts), dt, nsteps, h, hE, u, tr)
+
+
+def ocean_oracle_by_levels(level, f, opts, dt, nsteps, h, hE, u, tr, blocks):
+    """The oracle's ocean run (apps/ocean/run.cc:10-50) on a level-`level`
+    sphere, computed as `blocks` blocks of levels in parallel processes.  The
+    ocean app couples no levels (every task's level loop is independent) and
+    full columns give every level the same statics, so each block runs as a
+    column of its own levels with the statics cut to them -- identical to the
+    whole run value for value."""
+    import multiprocessing as mp
+    L = h.shape[1]
+    edges = np.linspace(0, L, blocks + 1).astype(int)
+    jobs = []
+    for a, b in zip(edges[:-1], edges[1:]):
+        fs = dict(f)
+        fs["maxLevelCell"] = np.full_like(f["maxLevelCell"], b - a)
+        fs["maxLevelEdgeTop"] = np.full_like(f["maxLevelEdgeTop"], b - a)
+        fs["highOrderAdvMask"] = np.ascontiguousarray(f["highOrderAdvMask"][:, a:b])
+        cut = lambda x: np.ascontiguousarray(x[:, a:b])  # noqa: E731
+        jobs.append((level, fs, opts, dt, nsteps, cut(h), cut(hE), cut(u), cut(tr),
+                     os.path.join(os.path.dirname(GOLDEN), "..", "oracle")))
+    with mp.get_context("spawn").Pool(min(blocks, os.cpu_count() or 1)) as pool:
+        parts = pool.map(_ocean_slice, jobs)
+    return np.concatenate(parts, axis=1)
