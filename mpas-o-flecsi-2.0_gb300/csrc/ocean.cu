@@ -111,8 +111,9 @@ __global__ void __launch_bounds__(TPB) k_oc_edges(DMesh m, DStat st, Stage S, in
     const double dv = m.dvEdge[e];
     // LO = dv (max(0, f) tr1 + min(0, f) tr2): one of the two products is a zero
     const bool up1 = dgt0(f);
-    // tracerWeight of solve.cc:222-223, zero on edges whose high-order mask is set
-    const double tw = (double)((mask + 1) & 1) * (dv * 0.5) * f;
+    // tracerWeight of solve.cc:222-223 is a zero on edges whose high-order mask
+    // is set (their high-order flux gains nothing); on the others the centred flux
+    const double tw = mask ? 0.0 : (double)((mask + 1) & 1) * (dv * 0.5) * f;
 #pragma unroll
     for (int t = 0; t < T; ++t) {
       const double lo = dv * (f * (up1 ? t1[t] : t2[t]));

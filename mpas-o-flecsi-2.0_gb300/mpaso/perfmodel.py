@@ -146,25 +146,35 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
 
 
 def ocean_kernels(d: Dims, fct=True, hmix=True):
-    """Per-launch (bytes, fp64 instructions) of the three ocean stage kernels."""
+    """Per-launch (bytes, fp64 instructions) of the three ocean stage kernels.
+    They keep the reference's rounding (no contracted multiply-adds), so every
+    stencil term is a multiply and an add."""
     nC, nE, L, T = d.nC, d.nE, d.L, d.T
     Na, Nc = d.maxAdv, d.avgEoC
     cl, el = nC * L, nE * L
     slot_c = Nc * nC
-    b1 = 8 * nE + 8 * el + 8 * cl * T + 8 * nE + 8 * el  # coe, F, tr_in, dv, hE
-    f1 = el
+    b1 = 8 * nE + 8 * el * T  # coe, tr_in (two cells)
+    f1 = 0
     if fct:
-        b1 += 12 * Na * nE + 4 * el + 16 * el * T
-        f1 += el * (1 + T * (Na + 5))
+        # F, advCells + one coefficient pair per slot, hoMask, dv, LO, A
+        b1 += 8 * el + 20 * Na * nE + 4 * el + 8 * nE + 16 * el * T
+        # wgt, a weight per slot, per tracer a multiply and an add per slot, LO (2),
+        # A (1), the centred-flux weight (3)
+        f1 += el * (1 + Na + 3 + T * (2 * Na + 3))
     if hmix:
-        b1 += 8 * nE + 8 * el * T
-        f1 += el * (1 + 2 * T)
+        b1 += 8 * nE + 8 * el + 8 * el * T  # rho, hE, DF
+        f1 += el * 3 * T
     b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
     b2 += 16 * el * T + 24 * cl * T
-    f2 = cl * (2 + T * (2 * Nc + 7 + 2.5))
-    b3 = 4 * nC + 12 * slot_c + 8 * nC + 8 * nE + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
+    # per slot and tracer: LO and A scaled by 1/area and summed (4); trUp (4), the
+    # new max / min (6), numerators and denominators (6), the two quotients where
+    # a bound is active (about a quarter of the cells)
+    f2 = cl * T * (4 * Nc + 16 + 5) if fct else 0
+    b3 = 4 * nC + 12 * slot_c + 8 * nC + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
     b3 += 8 * el * T * (int(fct) + int(hmix))
-    f3 = cl * T * (Nc * (1 + int(fct)) + 2.75)
+    # per slot and tracer: the limited flux, its 1/area scaling and sum (3), the
+    # del2 term (2); step_tracers_forward (4)
+    f3 = cl * T * ((3 * Nc if fct else 0) + (2 * Nc if hmix else 0) + 4)
     return {"oc_edges": (b1, f1), "oc_cells": (b2, f2), "oc_final": (b3, f3)}
 
 

