@@ -347,6 +347,35 @@ int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, con
                           double *gh0, double *gu0, double *gtr0);
 int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);
 
+/* ------------------------------------------------------------------------
+ * Test cases on the device.  The reference sets up its test cases and
+ * computes their error norms as host tasks: apps/sw/tasks/testcase.cc:37-227
+ * (Williamson cases 1, 5, 6) with compute_error (apps/sw/tasks/solve.cc:404-436),
+ * and apps/ocean/tasks/testcase.cc:96-294 (cases 1-3, calc_error_case_1/2/3).
+ * These entries do the same on a state's device fields.  The geometry they
+ * read is given once per mesh context, in reference numbering (host or
+ * device arrays; for an ensemble context, the members' arrays concatenated). */
+typedef struct {
+  const double *latCell, *lonCell;     /* [nCells] */
+  const double *latVertex, *lonVertex; /* [nVertices] */
+  const double *latEdge, *lonEdge, *angleEdge; /* [nEdges] */
+  const double *xCell, *yCell, *zCell; /* [nCells] */
+} mpaso_geometry;
+int mpaso_mesh_set_geometry(mpaso_mesh m, const mpaso_geometry *g);
+
+/* Writes the test case's initial h, u and tracers into the state (every
+ * level gets the reference's level-0 fields; tracers the case does not set
+ * are zero).  sw state: cases 1, 5, 6 (case 5 also sets the state's bottom
+ * topography, the mountain); ocean state: cases 1, 2, 3 (h = 1,
+ * layerThicknessEdge = 1; `coef` is case 3's del2 coefficient). */
+int mpaso_state_setup_case(mpaso_state s, int32_t test_case, double coef);
+/* Error norms of the state against the case's analytic solution after
+ * `elapsed` seconds, level 0 and tracer 0: err[0] = the reference's norm
+ * (sw case 1: the normalised l2 error of h; ocean: sqrt(sum err^2) / nCells of
+ * the pointwise relative error), err[1] = the largest pointwise relative
+ * error. */
+int mpaso_state_case_error(mpaso_state s, int32_t test_case, double elapsed, double coef, double *err);
+
 /* Device / runtime queries (no GPU needed: report 0 devices). */
 int mpaso_device_count(int32_t *n);
 const char *mpaso_build_info(void);

@@ -100,6 +100,10 @@ struct MeshCtx {
   void *ensure_scratch(size_t bytes);
   // ensemble contexts: first cell / edge / vertex of each member (n + 1 rows)
   std::vector<int64_t> members;
+  // geometry of the test-case initialisers (mpaso_mesh_set_geometry): latCell,
+  // lonCell, latVertex, lonVertex, latEdge, lonEdge, angleEdge, xCell, yCell,
+  // zCell back to back in the context numbering; null until set
+  double *geo = nullptr;
   ~MeshCtx();
 };
 

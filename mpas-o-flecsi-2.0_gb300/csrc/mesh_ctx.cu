@@ -14,6 +14,7 @@ namespace mpaso {
 MeshCtx::~MeshCtx() {
   if (arena) cudaFree(arena);
   if (scratch) cudaFree(scratch);
+  if (geo) cudaFree(geo);
   for (auto &p : d_perm)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);

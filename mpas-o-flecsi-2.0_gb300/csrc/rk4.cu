@@ -346,6 +346,7 @@ SwState::~SwState() {
   if (out_ready) cudaEventDestroy(out_ready);
   if (out_stream) cudaStreamDestroy(out_stream);
   if (io_stage) cudaFree(io_stage);
+  if (aux) cudaFree(aux);
   if (tune_l2) {  // hand the persisting L2 lines back
     cudaCtxResetPersistingL2Cache();
     cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);

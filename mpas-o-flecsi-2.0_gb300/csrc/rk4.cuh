@@ -178,6 +178,9 @@ struct SwState {
   // threads, limiter in its own kernel) instead of three
   int tune_split = 0;
   double *HPW = nullptr;
+  // small device buffer of the test-case set-up and error norms (testcases.cu)
+  double *aux = nullptr;
+  size_t aux_bytes = 0;
   ~SwState();
 };
 

@@ -34,6 +34,11 @@ class MeshDesc(ctypes.Structure):
                 + [(n, _dp) for n in ("edgeSignOnCell", "advCoef", "advCoef_3rd", "meshScalingDel2")])
 
 
+class Geometry(ctypes.Structure):
+    _fields_ = [(n, _dp) for n in ("latCell", "lonCell", "latVertex", "lonVertex", "latEdge", "lonEdge",
+                                   "angleEdge", "xCell", "yCell", "zCell")]
+
+
 class Params(ctypes.Structure):
     _fields_ = [("app", ctypes.c_int32), ("nlev", ctypes.c_int32), ("ntr", ctypes.c_int32),
                 ("gravity", ctypes.c_double), ("fct", ctypes.c_int32), ("hmix", ctypes.c_int32),
@@ -167,6 +172,16 @@ class DeviceMesh:
         check(lib().mpaso_mesh_device_bytes(self._h, ctypes.byref(b)))
         return b.value
 
+    def set_geometry(self, meshes):
+        """Geometry of the device test cases (mpaso_mesh_set_geometry) from one
+        mesh's fields, or from a list of members' (concatenated)."""
+        ms = meshes if isinstance(meshes, (list, tuple)) else [meshes]
+        names = ("latCell", "lonCell", "latVertex", "lonVertex", "latEdge", "lonEdge", "angleEdge",
+                 "xCell", "yCell", "zCell")
+        arrs = [np.ascontiguousarray(np.concatenate([m.fields[n] for m in ms]), np.float64) for n in names]
+        g = Geometry(*[_np_ptr(a, _dp) for a in arrs])
+        check(lib().mpaso_mesh_set_geometry(self._h, ctypes.byref(g)))
+
     # ---- per-task entries: return outputs as new numpy arrays ----
     def _call(self, name, *args):
         conv = [self._h]
@@ -282,6 +297,19 @@ class State:
         s = ctypes.c_void_p()
         check(lib().mpaso_state_stream(self._h, ctypes.byref(s)))
         return s.value
+
+    def setup_case(self, case, coef=0.0):
+        """The reference test case's initial fields, written on the device
+        (mpaso_state_setup_case; the mesh needs set_geometry first)."""
+        check(lib().mpaso_state_setup_case(self._h, int(case), ctypes.c_double(coef)))
+
+    def case_error(self, case, elapsed, coef=0.0):
+        """(reference norm, largest pointwise relative error) of the state
+        against the case's analytic solution (mpaso_state_case_error)."""
+        err = (ctypes.c_double * 2)()
+        check(lib().mpaso_state_case_error(self._h, int(case), ctypes.c_double(elapsed), ctypes.c_double(coef),
+                                           err))
+        return float(err[0]), float(err[1])
 
     def profile(self, dt, nsteps):
         """Mean ms per launch of each stage kernel kind: dict name -> ms."""
