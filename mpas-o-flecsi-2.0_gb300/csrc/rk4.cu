@@ -52,12 +52,12 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
   const int64_t nEL = (int64_t)m.nE * L;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nEL; i += (int64_t)gridDim.x * blockDim.x) {
     const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
-    const int2 c = m.coe[e];
-    const int2 v = m.voe[e];
+    const int2 c = __ldcs(&m.coe[e]);
+    const int2 v = __ldcs(&m.voe[e]);
     const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-    const double hs = S.h_in[i1] + S.h_in[i2];  // 2 h_edge
-    const double F = S.u_in[i] * hs;            // 2 u h_edge
-    const double pv2 = S.pv[(int64_t)v.x * L + k] + S.pv[(int64_t)v.y * L + k];  // 2 pv_edge
+    const double hs = __ldg(&S.h_in[i1]) + __ldg(&S.h_in[i2]);  // 2 h_edge
+    const double F = __ldg(&S.u_in[i]) * hs;                     // 2 u h_edge
+    const double pv2 = __ldg(&S.pv[(int64_t)v.x * L + k]) + __ldg(&S.pv[(int64_t)v.y * L + k]);  // 2 pv_edge
     S.FG[i] = make_double2(F, F * pv2);
     S.pve[i] = pv2;
     if constexpr (T > 0) edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, F, hs, st.dvh, st.cpm2, st.kdh);
@@ -81,8 +81,8 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
     const int ne = NW > 0 ? NW : m.maxEoE;
 #pragma unroll
     for (int j = 0; j < ne; ++j) {
-      const int eo = m.eoe[(int64_t)j * m.nE + e];
-      const double w = st.woe8[(int64_t)j * m.nE + e];
+      const int eo = __ldcs(&m.eoe[(int64_t)j * m.nE + e]);
+      const double w = __ldcs(&st.woe8[(int64_t)j * m.nE + e]);
       const int64_t io = (int64_t)eo * L + k;
       const double2 fg = S.FG[io];
       s1 = fma(w, fg.x, s1);

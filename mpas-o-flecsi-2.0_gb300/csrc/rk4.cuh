@@ -220,8 +220,8 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
                                                    const double *kd) {
   double t1[T], t2[T];
 #pragma unroll
-  for (int t = 0; t < T; ++t) t1[t] = S.tr_in[i1 * T + t], t2[t] = S.tr_in[i2 * T + t];
-  const double dvF = dv[e] * F;
+  for (int t = 0; t < T; ++t) t1[t] = __ldg(&S.tr_in[i1 * T + t]), t2[t] = __ldg(&S.tr_in[i2 * T + t]);
+  const double dvF = __ldcs(&dv[e]) * F;
   if (S.fct) {
     // low order: dv (max(0,F) tr1 + min(0,F) tr2) == dv F tr_upwind (ocean solve.cc:110-113)
     const bool up1 = dgt0(F);
@@ -233,20 +233,31 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
     const int na = NA > 0 ? NA : m.maxAdv;
 #pragma unroll
     for (int a = 0; a < na; ++a) {
-      const int cell = m.advCells[(int64_t)a * m.nE + e];
-      const double2 c2 = cpm[(int64_t)a * m.nE + e];
+      const int cell = __ldcs(&m.advCells[(int64_t)a * m.nE + e]);
+      const double2 c2 = __ldcs(&cpm[(int64_t)a * m.nE + e]);
       const double cf = neg ? c2.y : c2.x;
       const double *tr = S.tr_in + ((int64_t)cell * L + k) * T;
 #pragma unroll
-      for (int t = 0; t < T; ++t) s[t] = fma(cf, tr[t], s[t]);
+      for (int t = 0; t < T; ++t) s[t] = fma(cf, __ldg(&tr[t]), s[t]);
     }
-    const int mask = m.hoMask[(int64_t)e * m.fctLev + k];
+    const int mask = __ldcs(&m.hoMask[(int64_t)e * m.fctLev + k]);
+    // A = HO - LO, HO = F s; edges without the high-order mask take the centred
+    // flux (solve.cc:222-225).  A branch, not a select: the mask is set almost
+    // everywhere, and the centred flux would cost three more FP64 instructions
+    if (mask) {
 #pragma unroll
-    for (int t = 0; t < T; ++t) {
-      const double lo = dvF * (up1 ? t1[t] : t2[t]);
-      S.LO[i * T + t] = lo;
-      // A = HO - LO, HO = F s (masked edges: the centred flux, solve.cc:222-225)
-      S.A[i * T + t] = mask ? fma(F, s[t], -lo) : fma(0.5 * dvF, t1[t] + t2[t], -lo);
+      for (int t = 0; t < T; ++t) {
+        const double lo = dvF * (up1 ? t1[t] : t2[t]);
+        S.LO[i * T + t] = lo;
+        S.A[i * T + t] = fma(F, s[t], -lo);
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const double lo = dvF * (up1 ? t1[t] : t2[t]);
+        S.LO[i * T + t] = lo;
+        S.A[i * T + t] = fma(0.5 * dvF, t1[t] + t2[t], -lo);
+      }
     }
   } else if (S.centred) {
     // centred flux of compute_scalar_tend (apps/sw/tasks/solve.cc:255-269)
@@ -258,7 +269,7 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
     for (int t = 0; t < T; ++t) S.LO[i * T + t] = 0.0;
   }
   if (S.hmix) {
-    const double hk = hx * kd[e];
+    const double hk = hx * __ldcs(&kd[e]);
 #pragma unroll
     for (int t = 0; t < T; ++t) S.DF[i * T + t] = hk * (t2[t] - t1[t]);
   }
