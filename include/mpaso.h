@@ -347,6 +347,18 @@ int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, con
                           double *gh0, double *gu0, double *gtr0);
 int mpaso_adjoint_device_bytes(mpaso_state s, int64_t *bytes);
 
+/* nsteps RK4 steps of an sw state (any context, ensembles included; up to
+ * 3 tracers) in ONE persistent cooperative launch: a grid the SMs hold at
+ * once loops over the steps, stages and the three phases of each stage, with
+ * a grid barrier between phases.  No counterpart in the reference.  Every
+ * barrier wait is bounded: after `spin_limit` polls (0: 2^26, seconds) it
+ * gives up and the call returns MPASO_ERR_TIMEOUT, the state then partly
+ * advanced.  `extra_arrivals` must be 0 in use; a positive value makes every
+ * wait expect arrivals that never come, which exercises that bound.  Same
+ * results as mpaso_rk4_step_graph. */
+int mpaso_rk4_step_persistent(mpaso_state s, double dt, int32_t nsteps, int64_t spin_limit,
+                              int32_t extra_arrivals);
+
 /* ------------------------------------------------------------------------
  * Test cases on the device.  The reference sets up its test cases and
  * computes their error norms as host tasks: apps/sw/tasks/testcase.cc:37-227

@@ -43,6 +43,22 @@ constexpr int kOccMaxT = 1;  // OC = 1 variants exist up to this many tracers (b
 
 
 // ------------------------------------------------------------- K1: edges
+// One edge-level of the pre-pass.  RO: inputs through the read-only path
+// (false inside the persistent kernel).
+template <int T, int NW, bool RO>
+__device__ __forceinline__ void edge_pre_item(const DMesh &m, const DStat &st, const Stage &S, int L, int64_t i) {
+  const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
+  const int2 c = __ldcs(&m.coe[e]);
+  const int2 v = __ldcs(&m.voe[e]);
+  const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
+  const double hs = ld_in<RO>(&S.h_in[i1]) + ld_in<RO>(&S.h_in[i2]);  // 2 h_edge
+  const double F = ld_in<RO>(&S.u_in[i]) * hs;                         // 2 u h_edge
+  const double pv2 = ld_in<RO>(&S.pv[(int64_t)v.x * L + k]) + ld_in<RO>(&S.pv[(int64_t)v.y * L + k]);  // 2 pv_edge
+  S.FG[i] = make_double2(F, F * pv2);
+  S.pve[i] = pv2;
+  if constexpr (T > 0) edge_tracer_fluxes<T, NW, RO>(m, S, L, e, k, i, i1, i2, F, hs, st.dvh, st.cpm2, st.kdh);
+}
+
 template <int T, int NW, int OC>
 __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L) {
   stage_prologue();
@@ -50,18 +66,8 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
   // at once, so the work ends without a partial last wave (measured 37.4 ->
   // 36.0 us at level 7; the mixed edge / cell kernels below lost this way)
   const int64_t nEL = (int64_t)m.nE * L;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nEL; i += (int64_t)gridDim.x * blockDim.x) {
-    const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
-    const int2 c = __ldcs(&m.coe[e]);
-    const int2 v = __ldcs(&m.voe[e]);
-    const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
-    const double hs = __ldg(&S.h_in[i1]) + __ldg(&S.h_in[i2]);  // 2 h_edge
-    const double F = __ldg(&S.u_in[i]) * hs;                     // 2 u h_edge
-    const double pv2 = __ldg(&S.pv[(int64_t)v.x * L + k]) + __ldg(&S.pv[(int64_t)v.y * L + k]);  // 2 pv_edge
-    S.FG[i] = make_double2(F, F * pv2);
-    S.pve[i] = pv2;
-    if constexpr (T > 0) edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, F, hs, st.dvh, st.cpm2, st.kdh);
-  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nEL; i += (int64_t)gridDim.x * blockDim.x)
+    edge_pre_item<T, NW, true>(m, st, S, L, i);
 }
 
 // ------------------------------------------------------ K2: edges + cells
@@ -69,10 +75,8 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
 // edge threads here add the tracer fluxes (their stencil gathers overlap the
 // TRiSK arithmetic) and the cell threads leave the limiter, which needs every
 // edge's fluxes, to k_sw_limit.  Same arithmetic either way.
-template <int T, int NW, int OC, int SPLIT>
-__global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
-  stage_prologue();
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+template <int T, int NW, int SPLIT>
+__device__ __forceinline__ void tend_item(const DMesh &m, const DStat &st, const Stage &S, int L, int64_t i) {
   const int64_t nEL = (int64_t)m.nE * L;
   if (i < nEL) {
     const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
@@ -154,6 +158,12 @@ __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   }
 }
 
+template <int T, int NW, int OC, int SPLIT>
+__global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
+  stage_prologue();
+  tend_item<T, NW, SPLIT>(m, st, S, L, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Limiter kernel of the four-launch schedule: bounds, upwind tendency and
 // R+- of every cell from the fluxes k_sw_tend<.., SPLIT = 1> wrote.
 template <int T, int NC, int OC>
@@ -222,10 +232,8 @@ __device__ __forceinline__ void vertex_diag(const DMesh &m, const DStat &st, con
 }
 
 // ------------------------------------------------------ K3: cells + vertices
-template <int T, int NC, int OC>
-__global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
-  stage_prologue();
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+template <int T, int NC>
+__device__ __forceinline__ void final_item(const DMesh &m, const DStat &st, const Stage &S, int L, int64_t i) {
   const int64_t nCL = (int64_t)m.nC * L;
   const double *u_next = S.stage == 3 ? S.u_new : S.u_out;
   const double *h_next = S.stage == 3 ? S.h_new : S.h_out;
@@ -268,6 +276,12 @@ __global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
   vertex_diag(m, st, S, L, v, k, i, u_next, h_next);
 }
 
+template <int T, int NC, int OC>
+__global__ void MPASO_BOUNDS(OC) k_sw_final(DMesh m, DStat st, Stage S, int L) {
+  stage_prologue();
+  final_item<T, NC>(m, st, S, L, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+}
+
 // Initial diagnostics (apps/sw/run.cc:88-92).
 // NC = 6: the cell loops unrolled for meshes of at most hexagons (as k_sw_final's unrolled variant)
 template <int NC>
@@ -283,6 +297,67 @@ __global__ void __launch_bounds__(TPB) k_sw_diag(DMesh m, DStat st, Stage S, int
   if (i >= (int64_t)m.nV * L) return;
   const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
   vertex_diag(m, st, S, L, v, k, i, S.u_in, S.h_in);
+}
+
+// ------------------------------------------------- persistent RK4 steps
+// The whole run in one cooperative launch: every block of a grid the SMs hold
+// at once loops over the steps, the RK stages and the three phases of a stage
+// (the work of K1, K2, K3 above, grid-stride over the union of all members'
+// entities), with a grid barrier between phases.  Loads of values an earlier
+// phase wrote are plain (coherent) loads.
+struct StageSet {
+  Stage s[4];
+};
+
+// Grid barrier state: count[0] counts arrivals, count[1] is the error flag.
+// Every wait is bounded: after `spin` polls it sets the flag and gives up,
+// and a waiting block gives up as soon as it sees the flag, so the launch
+// always ends.  `extra` arrivals beyond the grid are waited for too: 0 in use,
+// > 0 only to make the waits run out on purpose (the test of the bound).
+struct GridBar {
+  unsigned int *count;
+  long long spin;
+  unsigned int extra;
+};
+
+__device__ bool grid_barrier(const GridBar &b, unsigned int &phase) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *cnt = b.count;
+    const unsigned int target = (phase + 1) * (gridDim.x + b.extra);
+    __threadfence();  // this block's writes before the arrival
+    atomicAdd(b.count, 1u);
+    long long polls = 0;
+    while (cnt[0] < target) {
+      if (cnt[1] || ++polls > b.spin) {
+        atomicExch(b.count + 1, 1u);
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();  // the other blocks' writes after it
+  }
+  __syncthreads();
+  ++phase;
+  return ((volatile unsigned int *)b.count)[1] == 0;
+}
+
+template <int T, int NW, int NC>
+__global__ void __launch_bounds__(TPB) k_sw_persistent(DMesh m, DStat st, StageSet P, int L, int nsteps,
+                                                       GridBar b) {
+  unsigned int phase = 0;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.x * blockDim.x;
+  const int64_t n1 = (int64_t)m.nE * L, n2 = ((int64_t)m.nE + m.nC) * L, n3 = ((int64_t)m.nC + m.nV) * L;
+  for (int step = 0; step < nsteps; ++step)
+    for (int rk = 0; rk < 4; ++rk) {
+      const Stage &S = P.s[rk];
+      for (int64_t i = tid; i < n1; i += nt) edge_pre_item<T, NW, false>(m, st, S, L, i);
+      if (!grid_barrier(b, phase)) return;
+      for (int64_t i = tid; i < n2; i += nt) tend_item<T, NW, 0>(m, st, S, L, i);
+      if (!grid_barrier(b, phase)) return;
+      for (int64_t i = tid; i < n3; i += nt) final_item<T, NC>(m, st, S, L, i);
+      if (!grid_barrier(b, phase)) return;
+    }
 }
 
 // Derived statics of a state.
@@ -347,6 +422,7 @@ SwState::~SwState() {
   if (out_stream) cudaStreamDestroy(out_stream);
   if (io_stage) cudaFree(io_stage);
   if (aux) cudaFree(aux);
+  if (pbar) cudaFree(pbar);
   if (tune_l2) {  // hand the persisting L2 lines back
     cudaCtxResetPersistingL2Cache();
     cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
@@ -570,6 +646,63 @@ void sw_steps(SwState &s, double dt, int nsteps, cudaStream_t st) {
   for (int n = 0; n < nsteps; ++n)
     for (int rk = 0; rk < 4; ++rk) launch_stage(s, make_stage(s, rk, dt), st);
   MPASO_CUDA(cudaGetLastError());
+}
+
+template <int T, int NW, int NC>
+void launch_persistent_T(SwState &s, const StageSet &P, int nsteps, GridBar b) {
+  const DMesh &m = s.mesh->ctx.d;
+  auto kern = k_sw_persistent<T, NW, NC>;
+  int per_sm = 0;
+  MPASO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPB, 0));
+  require(per_sm > 0, MPASO_ERR_CUDA, "persistent kernel does not fit an SM");
+  const int64_t need = blocks_for(((int64_t)m.nE + m.nC) * s.L, TPB);
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * s.mesh->ctx.sms, need));
+  DMesh mm = m;
+  DStat dd = s.st;
+  StageSet pp = P;
+  int L = s.L;
+  void *args[] = {&mm, &dd, &pp, &L, &nsteps, &b};
+  MPASO_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(TPB), args, 0, s.stream));
+}
+
+template <int T> void launch_persistent(SwState &s, const StageSet &P, int nsteps, GridBar b) {
+  const DMesh &m = s.mesh->ctx.d;
+  const bool w10 = m.maxEoE == 10 && (m.maxAdv == 10 || !s.p.fct || T == 0), c6 = m.maxEoC <= 6;
+  if (w10 && c6)
+    launch_persistent_T<T, 10, 6>(s, P, nsteps, b);
+  else
+    launch_persistent_T<T, 0, 0>(s, P, nsteps, b);
+}
+
+// nsteps RK4 steps in one persistent launch; MPASO_ERR_TIMEOUT when a grid
+// barrier gave up (the state is then partly advanced).
+void sw_steps_persistent(SwState &s, double dt, int nsteps, long long spin, unsigned int extra) {
+  require(s.p.app == MPASO_APP_SW, MPASO_ERR_ARG, "the persistent step is the sw app's");
+  require(nsteps >= 0, MPASO_ERR_ARG, "nsteps < 0");
+  if (nsteps == 0) return;
+  ensure_diag(s, s.stream);
+  if (!s.pbar) {
+    if (cudaMalloc(&s.pbar, 2 * sizeof(unsigned int)) != cudaSuccess) {
+      cudaGetLastError();
+      s.pbar = nullptr;
+      fail(MPASO_ERR_ALLOC, "device allocation of the grid barrier failed");
+    }
+  }
+  MPASO_CUDA(cudaMemsetAsync(s.pbar, 0, 2 * sizeof(unsigned int), s.stream));
+  StageSet P;
+  for (int rk = 0; rk < 4; ++rk) P.s[rk] = make_stage(s, rk, dt);
+  GridBar b{s.pbar, spin > 0 ? spin : (1LL << 26), extra};
+  switch (s.T) {
+    case 0: launch_persistent<0>(s, P, nsteps, b); break;
+    case 1: launch_persistent<1>(s, P, nsteps, b); break;
+    case 2: launch_persistent<2>(s, P, nsteps, b); break;
+    case 3: launch_persistent<3>(s, P, nsteps, b); break;
+    default: fail(MPASO_ERR_ARG, "the persistent step supports up to 3 tracers");
+  }
+  unsigned int flag[2] = {0, 0};
+  MPASO_CUDA(cudaMemcpyAsync(flag, s.pbar, sizeof(flag), cudaMemcpyDeviceToHost, s.stream));
+  MPASO_CUDA(cudaStreamSynchronize(s.stream));
+  require(flag[1] == 0, MPASO_ERR_TIMEOUT, "a grid barrier of the persistent step gave up waiting");
 }
 
 }  // namespace
@@ -1275,6 +1408,17 @@ int mpaso_state_profile(mpaso_state s, double dt, int32_t nsteps, double *ms_per
       std::strncpy(names, kinds, (size_t)names_len - 1);
       names[names_len - 1] = 0;
     }
+  });
+}
+
+int mpaso_rk4_step_persistent(mpaso_state s, double dt, int32_t nsteps, int64_t spin_limit,
+                              int32_t extra_arrivals) {
+  return guarded("mpaso_rk4_step_persistent", [&] {
+    require(s != nullptr, MPASO_ERR_ARG, "null state");
+    require(extra_arrivals >= 0, MPASO_ERR_ARG, "extra_arrivals < 0");
+    SwState &S = s->s;
+    MPASO_CUDA(cudaSetDevice(S.mesh->ctx.device));
+    sw_steps_persistent(S, dt, nsteps, spin_limit, (unsigned int)extra_arrivals);
   });
 }
 

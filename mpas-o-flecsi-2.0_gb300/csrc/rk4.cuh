@@ -25,6 +25,16 @@ __device__ __forceinline__ double rcp_nr(double b) {
 
 __device__ __forceinline__ long long sign_mask(double s) { return dbits(s) & kSignBit; }
 
+// Load of a value an earlier kernel wrote: through the read-only
+// (non-coherent) path when RO, else a plain load -- inside the persistent
+// kernel, where an earlier phase of the same launch wrote it.
+template <bool RO, class V> __device__ __forceinline__ V ld_in(const V *p) {
+  if constexpr (RO)
+    return __ldg(p);
+  else
+    return *p;
+}
+
 // Programmatic dependent launch: a kernel launched with the
 // programmatic-serialization attribute may be scheduled while its
 // predecessor's last blocks still run; it waits here (a hardware dependency,
@@ -178,6 +188,8 @@ struct SwState {
   // threads, limiter in its own kernel) instead of three
   int tune_split = 0;
   double *HPW = nullptr;
+  // grid barrier of the persistent step: arrival count, error flag
+  unsigned int *pbar = nullptr;
   // small device buffer of the test-case set-up and error norms (testcases.cu)
   double *aux = nullptr;
   size_t aux_bytes = 0;
@@ -213,14 +225,14 @@ void drop_adjoint_graph(SwState &s);
 // The thickness flux arrives as F = s * u h_e (s = 1 or 2) and the edge
 // thickness as hx = s * h_e; dv, cp, cm, kd are the matching 1/s copies.
 // NA > 0: compile-time advection-stencil width (the mesh's maxAdv); 0 = runtime.
-template <int T, int NA>
+template <int T, int NA, bool RO = true>
 __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &S, int L, int e, int k,
                                                    int64_t i, int64_t i1, int64_t i2, double F,
                                                    double hx, const double *dv, const double2 *cpm,
                                                    const double *kd) {
   double t1[T], t2[T];
 #pragma unroll
-  for (int t = 0; t < T; ++t) t1[t] = __ldg(&S.tr_in[i1 * T + t]), t2[t] = __ldg(&S.tr_in[i2 * T + t]);
+  for (int t = 0; t < T; ++t) t1[t] = ld_in<RO>(&S.tr_in[i1 * T + t]), t2[t] = ld_in<RO>(&S.tr_in[i2 * T + t]);
   const double dvF = __ldcs(&dv[e]) * F;
   if (S.fct) {
     // low order: dv (max(0,F) tr1 + min(0,F) tr2) == dv F tr_upwind (ocean solve.cc:110-113)
@@ -238,7 +250,7 @@ __device__ __forceinline__ void edge_tracer_fluxes(const DMesh &m, const Stage &
       const double cf = neg ? c2.y : c2.x;
       const double *tr = S.tr_in + ((int64_t)cell * L + k) * T;
 #pragma unroll
-      for (int t = 0; t < T; ++t) s[t] = fma(cf, __ldg(&tr[t]), s[t]);
+      for (int t = 0; t < T; ++t) s[t] = fma(cf, ld_in<RO>(&tr[t]), s[t]);
     }
     const int mask = __ldcs(&m.hoMask[(int64_t)e * m.fctLev + k]);
     // A = HO - LO, HO = F s; edges without the high-order mask take the centred

@@ -298,6 +298,11 @@ class State:
         check(lib().mpaso_state_stream(self._h, ctypes.byref(s)))
         return s.value
 
+    def step_persistent(self, dt, nsteps, spin_limit=0, extra_arrivals=0):
+        """nsteps RK4 steps in one persistent launch (mpaso_rk4_step_persistent)."""
+        check(lib().mpaso_rk4_step_persistent(self._h, ctypes.c_double(dt), int(nsteps),
+                                              ctypes.c_int64(spin_limit), int(extra_arrivals)))
+
     def setup_case(self, case, coef=0.0):
         """The reference test case's initial fields, written on the device
         (mpaso_state_setup_case; the mesh needs set_geometry first)."""

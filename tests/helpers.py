@@ -83,3 +83,26 @@ def ocean_oracle_by_levels(level, f, opts, dt, nsteps, h, hE, u, tr, blocks):
     with mp.get_context("spawn").Pool(min(blocks, os.cpu_count() or 1)) as pool:
         parts = pool.map(_ocean_slice, jobs)
     return np.concatenate(parts, axis=1)
+
+
+def extremum_distance(mesh, x):
+    """Rings from every cell to the nearest local extremum of the cell field x
+    (a cell whose value is >= or <= all of its neighbours'), by breadth-first
+    search over cellsOnCell."""
+    f = mesh.fields
+    coc = f["cellsOnCell"] - 1
+    n = f["nEdgesOnCell"]
+    valid = np.arange(coc.shape[1])[None, :] < n[:, None]
+    nb = np.where(valid, coc, np.arange(mesh.nCells)[:, None])
+    ext = np.all(x[:, None] >= x[nb], axis=1) | np.all(x[:, None] <= x[nb], axis=1)
+    dist = np.full(mesh.nCells, -1, np.int64)
+    front = np.flatnonzero(ext)
+    dist[front] = 0
+    d = 0
+    while front.size:
+        d += 1
+        cand = np.unique(nb[front][valid[front]])
+        cand = cand[dist[cand] < 0]
+        dist[cand] = d
+        front = cand
+    return dist
