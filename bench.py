@@ -795,7 +795,7 @@ def ensemble_arm(args):
         for f, k in ((G.FIELD_H, 0), (G.FIELD_U, 1), (G.FIELD_TRACERS, 2)):
             s.set(f, states[i][k])
         s.set_launch_config(launch["unroll"], launch["threads"], launch["capped"], 0, launch["overlap"],
-                            launch["split"])
+                            launch["split"], launch["lanes"])
         s.step_graph(dt, W)
         singles.append((d, s))
     torch.cuda.synchronize()

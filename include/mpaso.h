@@ -298,8 +298,17 @@ int mpaso_state_device_bytes(mpaso_state s, int64_t *bytes);
  * reservation. */
 int mpaso_state_launch_config(mpaso_state s, int32_t *config);
 int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config);
+/* The same with n >= 12 ints, the 13th being the threads per edge-level of
+ * the TRiSK loop in the second stage kernel (sw app, at most one tracer): 1,
+ * 2 or 4 lanes share an edge's stencil and add their partial sums by warp
+ * shuffles (results differ in the last bits).  Entries past 13 read as
+ * nothing and are written as 0.  The autotuner times the lane counts with
+ * the second kernel's other variants; the 12-int calls leave it as it is. */
+int mpaso_state_launch_config_ex(mpaso_state s, int32_t *config, int32_t n);
+int mpaso_state_set_launch_config_ex(mpaso_state s, const int32_t *config, int32_t n);
 /* Per-mesh autotuner: for each stage kernel in turn, times every variant
- * (unrolled or not x capped or not x 64/128/256 threads) over nsteps steps
+ * (unrolled or not x capped or not x 64/128/256 threads, and for the second
+ * kernel of the sw app 1, 2 or 4 threads per edge-level) over nsteps steps
  * of size dt and keeps the fastest, then picks the L2 residency choice on
  * the whole stage, the schedule on the whole stage and the launch overlap on
  * uninterrupted steps.  The prognostic state is saved first and restored on

@@ -39,6 +39,7 @@ constexpr int TPB = 256;
 // OC = 1: registers capped at 40 so 1536 threads fit an SM (more warps to hide
 // gather latency, less ILP per warp); OC = 0: the compiler's choice.
 constexpr int kOccMaxT = 1;  // OC = 1 variants exist up to this many tracers (beyond, they spill)
+constexpr int kLanesMaxT = 1;  // variants with 2 or 4 lanes per edge exist up to this many tracers
 #define MPASO_BOUNDS(OC) __launch_bounds__(TPB, (OC) ? 1536 / TPB : 0)
 
 
@@ -75,16 +76,33 @@ __global__ void MPASO_BOUNDS(OC) k_sw_edge_pre(DMesh m, DStat st, Stage S, int L
 // edge threads here add the tracer fluxes (their stencil gathers overlap the
 // TRiSK arithmetic) and the cell threads leave the limiter, which needs every
 // edge's fluxes, to k_sw_limit.  Same arithmetic either way.
-template <int T, int NW, int SPLIT>
+// LANES (1, 2 or 4) threads per edge-level share its TRiSK stencil: lane j
+// sums slots j, j + LANES, ..., and the partial sums meet by warp shuffles
+// (the sum is reassociated, so results differ in the last bits).  More lanes
+// mean more FP64 issue per edge (the edge's own arithmetic runs on every lane)
+// but more gathers in flight; they pay only where the mesh is too small to
+// fill the GPU, which the autotuner measures.
+template <int LANES> __device__ __forceinline__ double lane_total(double x) {
+  if constexpr (LANES > 1) {
+    const unsigned grp = (LANES == 2 ? 0x3u : 0xfu) << (threadIdx.x & 31 & ~(LANES - 1));
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) x += __shfl_xor_sync(grp, x, o);
+  }
+  return x;
+}
+
+template <int T, int NW, int SPLIT, int LANES = 1>
 __device__ __forceinline__ void tend_item(const DMesh &m, const DStat &st, const Stage &S, int L, int64_t i) {
   const int64_t nEL = (int64_t)m.nE * L;
-  if (i < nEL) {
+  if (i < nEL * LANES) {
+    const int lane = (int)(i & (LANES - 1));
+    i /= LANES;
     const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
     // q = sum_j W_j F_j (pv_e + pv_j) / 2 = (Pv_e sum W/8 F2_j + sum W/8 F2_j Pv_j)
     double s1 = 0.0, s2 = 0.0;
     const int ne = NW > 0 ? NW : m.maxEoE;
 #pragma unroll
-    for (int j = 0; j < ne; ++j) {
+    for (int j = lane; j < ne; j += LANES) {
       const int eo = __ldcs(&m.eoe[(int64_t)j * m.nE + e]);
       const double w = __ldcs(&st.woe8[(int64_t)j * m.nE + e]);
       const int64_t io = (int64_t)eo * L + k;
@@ -92,6 +110,9 @@ __device__ __forceinline__ void tend_item(const DMesh &m, const DStat &st, const
       s1 = fma(w, fg.x, s1);
       s2 = fma(w, fg.y, s2);
     }
+    s1 = lane_total<LANES>(s1);
+    s2 = lane_total<LANES>(s2);
+    if (lane) return;
     const double q = fma(S.pve[i], s1, s2);
     if (S.tape_s1) S.tape_s1[i] = s1;
     const int2 c = m.coe[e];
@@ -123,7 +144,7 @@ __device__ __forceinline__ void tend_item(const DMesh &m, const DStat &st, const
       edge_tracer_fluxes<T, NW>(m, S, L, e, k, i, i1, i2, S.FG[i].x, h1 + h2, st.dvh, st.cpm2, st.kdh);
     return;
   }
-  i -= nEL;
+  i -= nEL * LANES;
   if (i >= (int64_t)m.nC * L) return;
   constexpr int NC = NW > 0 ? 6 : 0;  // the unrolled variant also unrolls the cell loops
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
@@ -158,10 +179,10 @@ __device__ __forceinline__ void tend_item(const DMesh &m, const DStat &st, const
   }
 }
 
-template <int T, int NW, int OC, int SPLIT>
+template <int T, int NW, int OC, int SPLIT, int LANES = 1>
 __global__ void MPASO_BOUNDS(OC) k_sw_tend(DMesh m, DStat st, Stage S, int L) {
   stage_prologue();
-  tend_item<T, NW, SPLIT>(m, st, S, L, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  tend_item<T, NW, SPLIT, LANES>(m, st, S, L, blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
 }
 
 // Limiter kernel of the four-launch schedule: bounds, upwind tendency and
@@ -548,15 +569,26 @@ void launch_k1(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_
   launch_ex(kern, nres, b, win, s, st, m, s.st, S, s.L);
 }
 
+template <int T, int OC, int SPLIT, int LANES>
+void launch_k2_lanes(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t n = ((int64_t)m.nE * LANES + m.nC) * s.L;
+  const bool win = s.tune_l2 == 2;
+  if (unroll)
+    launch_ex(k_sw_tend<T, 10, OC, SPLIT, LANES>, n, b, win, s, st, m, s.st, S, s.L);
+  else
+    launch_ex(k_sw_tend<T, 0, OC, SPLIT, LANES>, n, b, win, s, st, m, s.st, S, s.L);
+}
+
 template <int T, int OC, int SPLIT>
 void launch_k2(const SwState &s, const Stage &S, bool unroll, int b, cudaStream_t st) {
   const DMesh &m = s.mesh->ctx.d;
-  const int64_t n = ((int64_t)m.nE + m.nC) * s.L;
-  const bool win = s.tune_l2 == 2;
-  if (unroll)
-    launch_ex(k_sw_tend<T, 10, OC, SPLIT>, n, b, win, s, st, m, s.st, S, s.L);
-  else
-    launch_ex(k_sw_tend<T, 0, OC, SPLIT>, n, b, win, s, st, m, s.st, S, s.L);
+  // several lanes per edge: the three-launch schedule with at most one tracer
+  if constexpr (!SPLIT && T <= kLanesMaxT) {
+    if (s.tune_lanes == 2) return launch_k2_lanes<T, OC, 0, 2>(s, S, unroll, b, st);
+    if (s.tune_lanes == 4) return launch_k2_lanes<T, OC, 0, 4>(s, S, unroll, b, st);
+  }
+  launch_k2_lanes<T, OC, SPLIT, 1>(s, S, unroll, b, st);
   if constexpr (SPLIT && T > 0) {
     const int64_t nc = (int64_t)m.nC * s.L;
     if (unroll)
@@ -960,6 +992,9 @@ void get_config(const SwState &S, int32_t *config) {
   config[10] = S.tune_pdl;
   config[11] = S.tune_split;
 }
+
+// Whether the state may run its TRiSK loop with several lanes per edge.
+bool has_lanes(const SwState &S) { return S.p.app == MPASO_APP_SW && S.T <= kLanesMaxT; }
 
 constexpr int kTpbChoices[3] = {64, 128, 256};
 
@@ -1481,6 +1516,28 @@ int mpaso_state_set_launch_config(mpaso_state s, const int32_t *config) {
   });
 }
 
+int mpaso_state_launch_config_ex(mpaso_state s, int32_t *config, int32_t n) {
+  return guarded("mpaso_state_launch_config_ex", [&] {
+    require(s && config && n >= 12, MPASO_ERR_ARG, "config needs at least 12 ints");
+    get_config(s->s, config);
+    if (n > 12) config[12] = s->s.tune_lanes;
+    for (int k = 13; k < n; ++k) config[k] = 0;
+  });
+}
+
+int mpaso_state_set_launch_config_ex(mpaso_state s, const int32_t *config, int32_t n) {
+  return guarded("mpaso_state_set_launch_config_ex", [&] {
+    require(s && config && n >= 12, MPASO_ERR_ARG, "config needs at least 12 ints");
+    const int lanes = n > 12 ? config[12] : 1;
+    require(lanes == 1 || lanes == 2 || lanes == 4, MPASO_ERR_ARG, "lanes per edge must be 1, 2 or 4");
+    require(lanes == 1 || has_lanes(s->s), MPASO_ERR_ARG,
+            "several lanes per edge need the sw app with at most one tracer");
+    const int rc = mpaso_state_set_launch_config(s, config);
+    if (rc != MPASO_OK) fail(rc, mpaso_last_error());
+    s->s.tune_lanes = lanes;
+  });
+}
+
 int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *config) {
   return guarded("mpaso_state_autotune", [&] {
     require(s && nsteps > 0 && dt > 0.0, MPASO_ERR_ARG, "bad argument");
@@ -1514,19 +1571,24 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
       time_stage_kernels(S, dt, 1, ms);  // warm-up
       for (int k = 0; k < 3; ++k) {
         double best = 1e300;
-        int best_u = S.tune_unroll[k], best_b = S.tune_tpb[k], best_o = S.tune_occ[k];
-        for (int u = has_unrolled(S, k) ? 1 : 0; u >= 0; --u)
-          for (int o = 0; o <= (has_capped(S) ? 1 : 0); ++o)
-            for (int b : kTpbChoices) {
-              S.tune_unroll[k] = u, S.tune_tpb[k] = b, S.tune_occ[k] = o;
-              // one untimed step first: a variant's first launch loads its code
-              save_restore(false);
-              time_stage_kernels(S, dt, 1, ms);
-              save_restore(false);
-              time_stage_kernels(S, dt, nsteps, ms);
-              if (ms[k] < best) best = ms[k], best_u = u, best_b = b, best_o = o;
-            }
+        int best_u = S.tune_unroll[k], best_b = S.tune_tpb[k], best_o = S.tune_occ[k], best_l = S.tune_lanes;
+        for (int lanes : {1, 2, 4}) {
+          if (lanes > 1 && (k != 1 || !has_lanes(S))) continue;
+          S.tune_lanes = lanes;
+          for (int u = has_unrolled(S, k) ? 1 : 0; u >= 0; --u)
+            for (int o = 0; o <= (has_capped(S) ? 1 : 0); ++o)
+              for (int b : kTpbChoices) {
+                S.tune_unroll[k] = u, S.tune_tpb[k] = b, S.tune_occ[k] = o;
+                // one untimed step first: a variant's first launch loads its code
+                save_restore(false);
+                time_stage_kernels(S, dt, 1, ms);
+                save_restore(false);
+                time_stage_kernels(S, dt, nsteps, ms);
+                if (ms[k] < best) best = ms[k], best_u = u, best_b = b, best_o = o, best_l = lanes;
+              }
+        }
         S.tune_unroll[k] = best_u, S.tune_tpb[k] = best_b, S.tune_occ[k] = best_o;
+        if (k == 1) S.tune_lanes = best_l;
       }
       // L2 persistence changes every kernel's hit rate: judged on the whole stage
       double best = 1e300;

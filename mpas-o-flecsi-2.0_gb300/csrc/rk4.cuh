@@ -188,6 +188,9 @@ struct SwState {
   // threads, limiter in its own kernel) instead of three
   int tune_split = 0;
   double *HPW = nullptr;
+  // threads per edge-level of the TRiSK loop in the second stage kernel (sw
+  // app, at most one tracer): 1, 2 or 4
+  int tune_lanes = 1;
   // grid barrier of the persistent step: arrival count, error flag
   unsigned int *pbar = nullptr;
   // small device buffer of the test-case set-up and error norms (testcases.cu)

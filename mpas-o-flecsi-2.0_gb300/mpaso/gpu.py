@@ -330,28 +330,29 @@ class State:
     def _cfg_dict(c):
         return {"unroll": [int(x) for x in c[:3]], "threads": [int(x) for x in c[3:6]],
                 "capped": [int(x) for x in c[6:9]], "l2": int(c[9]), "overlap": int(c[10]),
-                "split": int(c[11])}
+                "split": int(c[11]), "lanes": int(c[12])}
 
     def launch_config(self):
         """{'unroll', 'threads', 'capped'}: one value per stage kernel; 'l2': the
         static array kept resident in L2 (0 none, 1 advection coefficients, 2 TRiSK weights);
         'overlap': programmatic dependent launch between stage kernels; 'split': the
-        four-launch schedule (sw with tracers)."""
-        c = (ctypes.c_int32 * 12)()
-        check(lib().mpaso_state_launch_config(self._h, c))
+        four-launch schedule (sw with tracers); 'lanes': threads per edge-level of the
+        TRiSK loop (1, 2 or 4)."""
+        c = (ctypes.c_int32 * 13)()
+        check(lib().mpaso_state_launch_config_ex(self._h, c, 13))
         return self._cfg_dict(c)
 
-    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=0, split=0):
-        c = (ctypes.c_int32 * 12)(*[int(x) for x in list(unroll) + list(threads) + list(capped) +
-                                    [l2, overlap, split]])
-        check(lib().mpaso_state_set_launch_config(self._h, c))
+    def set_launch_config(self, unroll, threads, capped=(0, 0, 0), l2=0, overlap=0, split=0, lanes=1):
+        c = (ctypes.c_int32 * 13)(*[int(x) for x in list(unroll) + list(threads) + list(capped) +
+                                    [l2, overlap, split, lanes]])
+        check(lib().mpaso_state_set_launch_config_ex(self._h, c, 13))
 
     def autotune(self, dt, nsteps=3):
         """Times every launch variant of each stage kernel on this mesh and keeps
         the fastest; (h, u, tracers) are restored afterwards.  Returns the choice."""
         c = (ctypes.c_int32 * 12)()
         check(lib().mpaso_state_autotune(self._h, ctypes.c_double(dt), int(nsteps), c))
-        return self._cfg_dict(c)
+        return self.launch_config()
 
     # ---- differentiation (sw app: h and u) ----
     def forward(self, dt, nsteps, ckpt_every):

@@ -50,6 +50,27 @@ def test_every_launch_variant_matches_goldens(name, cfg):
 
 
 @pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("lanes", [2, 4])
+def test_lanes_per_edge_match_goldens(name, lanes):
+    """2 or 4 threads per edge-level in the TRiSK loop (sw app, at most one
+    tracer) keep the one-step parity bar; elsewhere the choice is refused."""
+    from mpaso._lib import MpasoError
+    g = Golden(name)
+    dm, st = make_state(g)
+    if g.app != "sw" or g.T > 1:
+        with pytest.raises(MpasoError):
+            st.set_launch_config([1, 1, 1], [256, 256, 256], lanes=lanes)
+        return
+    st.set_launch_config([1, 1, 1], [128, 128, 128], lanes=lanes)
+    assert st.launch_config()["lanes"] == lanes
+    st.step_graph(g.dt, 1)
+    for a, b in zip(_fields(st, g.app), [g["tr_1"], g["h_1"], g["u_1"]]):
+        assert rel_max(a, b) < TOL1
+    st.close()
+    dm.close()
+
+
+@pytest.mark.parametrize("name", golden_names())
 def test_block_size_is_bitwise_neutral(name):
     g = Golden(name)
     res = []
