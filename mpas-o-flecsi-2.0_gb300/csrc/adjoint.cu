@@ -178,11 +178,11 @@ __global__ void __launch_bounds__(TPB) k_adj_prep(DMesh m, AdjArgs a, int L) {
 
 // B1 (edges): transposed PV flux, d tend_h / dF, chain through F = u he.
 // NW = 10: the edgesOnEdge stencil unrolled at compile time (10-slot meshes).
+// `tr`: the tracer part's thickness-flux and edge-thickness cotangents lFt,
+// lhet of this edge (from TB) are added.
 template <int NW>
-__global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
-  stage_prologue();
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= (int64_t)m.nE * L) return;
+__device__ __forceinline__ void b1_item(const DMesh &m, const AdjArgs &a, int L, int64_t i, bool tr, double lFt,
+                                        double lhet) {
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
   // S1 = sum_j W_j F_j comes from the forward's tape (4 x its W/8 . 2F sum, exact)
   const double s1 = 4.0 * a.s1[i];
@@ -203,22 +203,29 @@ __global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
   const double dth = a.lk_h[i2] * m.invAreaCell[c.y] - a.lk_h[i1] * m.invAreaCell[c.x];
   double lF = fma(0.5, fma(pve, t1, t2), m.dvEdge[e] * dth);
   a.lpve[i] = 0.5 * fma(a.lk_u[i], s1, Fe * t1);
-  if (a.lFt) {
-    lF += a.lFt[i];
+  if (tr) {
+    lF += lFt;
     a.mu_u[i] = lF * he;
-    a.lhe[i] = fma(lF, ue, a.lhet[i]);
+    a.lhe[i] = fma(lF, ue, lhet);
   } else {
     a.mu_u[i] = lF * he;
     a.lhe[i] = lF * ue;
   }
 }
 
-// B2 (cells + vertices): gradient terms, h_e -> h, pv -> (circ, hs).
-__global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
+template <int NW>
+__global__ void __launch_bounds__(TPB) k_adj_b1(DMesh m, AdjArgs a, int L) {
   stage_prologue();
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t nCL = (int64_t)m.nC * L;
-  if (i < nCL) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nE * L) return;
+  const bool tr = a.lFt != nullptr;
+  b1_item<NW>(m, a, L, i, tr, tr ? a.lFt[i] : 0.0, tr ? a.lhet[i] : 0.0);
+}
+
+// B2 (cells + vertices): gradient terms, h_e -> h, pv -> (circ, hs).
+// `muh`: the tracer part's thickness cotangent of this cell (0 without tracers).
+__device__ __forceinline__ void b2_cell_item(const DMesh &m, const AdjArgs &a, int L, int64_t i, double muh) {
+  {
     const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
     double G = 0.0, sl = 0.0;
     auto slot = [&](int j, bool ok) {
@@ -232,13 +239,13 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
       for_slots<6>(m.nEoC[c], slot);
     else
       for_slots<0>(m.nEoC[c], slot);
-    a.mu_h[i] = fma(0.5, sl, -a.g * G) + (a.muh_t ? a.muh_t[i] : 0.0);
+    a.mu_h[i] = fma(0.5, sl, -a.g * G) + muh;
     a.lke[i] = -G;
     if (a.visc) a.ldiv[i] = a.nu * G;
-    return;
   }
-  i -= nCL;
-  if (i >= (int64_t)m.nV * L) return;
+}
+
+__device__ __forceinline__ void b2_vertex_item(const DMesh &m, const AdjArgs &a, int L, int64_t i) {
   const int v = (int)(i / L), k = (int)(i - (int64_t)v * L);
   double lpv = 0.0, lvort = 0.0;
 #pragma unroll
@@ -255,6 +262,18 @@ __global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
   if (a.visc) lc = fma(-a.nu * lvort, m.invAreaTriangle[v], lc);
   a.lcirc[i] = lc;
   a.lhs[i] = -lpv * a.pv[i] * rh;
+}
+
+__global__ void __launch_bounds__(TPB) k_adj_b2(DMesh m, AdjArgs a, int L) {
+  stage_prologue();
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (i < nCL) {
+    b2_cell_item(m, a, L, i, a.muh_t ? a.muh_t[i] : 0.0);
+    return;
+  }
+  i -= nCL;
+  if (i < (int64_t)m.nV * L) b2_vertex_item(m, a, L, i);
 }
 
 // RK4 cotangent bookkeeping for one element once mu is complete.
@@ -457,9 +476,8 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
 // tracer the parts for cells(e) go to p12 and lambda_HO F, split by the sign
 // of F, to lho (TC gathers them); per edge the thickness-flux and
 // edge-thickness cotangents summed over tracers go to lFt / lhet (B1 adds them).
-__global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= (int64_t)m.nE * L) return;
+__device__ __forceinline__ void tr_b_item(const DMesh &m, const TrArgs &a, int L, int64_t i, double &lF_out,
+                                          double &lhe_out) {
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L), T = a.T;
   const int2 c = m.coe[e];
   const int64_t i1 = (int64_t)c.x * L + k, i2 = (int64_t)c.y * L + k;
@@ -526,6 +544,14 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
     }
     a.p12[it] = make_double2(p1, p2);
   }
+  lF_out = lF, lhe_out = lhe;
+}
+
+__global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nE * L) return;
+  double lF, lhe;
+  tr_b_item(m, a, L, i, lF, lhe);
   if (a.ocean) return;
   a.lFt[i] = lF;
   a.lhet[i] = lhe;
@@ -537,12 +563,10 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_b(DMesh m, TrArgs a, int L) {
 // neighbours (DMesh::cocU); then q = h tr is converted and the RK bookkeeping
 // of q runs (g = lk_q / areaCell for the next stage beside it).  NL lanes per
 // cell split the gathers and sum by shuffles.
+// Returns true on the lane that holds the cell's thickness cotangent mh_out.
 template <int NL>
-__global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool tr_c_item(const DMesh &m, const TrArgs &a, int L, int64_t g, double &mh_out) {
   const int lane = (int)(g & (NL - 1));
-  const int64_t nCL = (int64_t)m.nC * L;
-  if (g / NL >= nCL) return;  // whole groups: all lanes of a live cell stay
   const int64_t i = g / NL;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c], T = a.T;
@@ -598,7 +622,43 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
     if (!a.ocean) mh = fma(-mq, a.tr[it], mh);
     a.gq[it] = combine(a.rk, a.dt, it, mq, a.lam_q, a.acc_q, a.lk_q) * inva;
   }
-  if (lane == 0 && !a.ocean) a.muh_t[i] = mh;
+  mh_out = mh;
+  return lane == 0;
+}
+
+template <int NL>
+__global__ void __launch_bounds__(TPB) k_adj_tr_c(DMesh m, TrArgs a, int L) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g / NL >= (int64_t)m.nC * L) return;  // whole groups: all lanes of a live cell stay
+  double mh;
+  if (tr_c_item<NL>(m, a, L, g, mh) && !a.ocean) a.muh_t[g / NL] = mh;
+}
+
+// The sw app with tracers, fused by item: TB and B1 of one edge-level in one
+// thread (the tracer part's flux cotangents pass in registers) ...
+template <int NW>
+__global__ void __launch_bounds__(TPB) k_adj_trb_b1(DMesh m, TrArgs t, AdjArgs a, int L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)m.nE * L) return;
+  double lF, lhe;
+  tr_b_item(m, t, L, i, lF, lhe);
+  b1_item<NW>(m, a, L, i, true, lF, lhe);
+}
+
+// ... and TC and B2: the NL lanes of a cell-level do TC, its first lane then
+// the cell part of B2 with the thickness cotangent in hand; the threads past
+// the cells do B2's vertices.
+template <int NL>
+__global__ void __launch_bounds__(TPB) k_adj_trc_b2(DMesh m, TrArgs t, AdjArgs a, int L) {
+  int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (g < nCL * NL) {
+    double mh;
+    if (tr_c_item<NL>(m, t, L, g, mh)) b2_cell_item(m, a, L, g / NL, mh);
+    return;
+  }
+  g -= nCL * NL;
+  if (g < (int64_t)m.nV * L) b2_vertex_item(m, a, L, g);
 }
 
 // Window ends: lambda_q = lambda_tr / h, lambda_h -= sum_t lambda_tr tr / h
@@ -729,15 +789,28 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
       else
         launch_pdl(k_adj_tr_a<NLA, 0>, nC * NLA, TPB, pdl, st, m, t, L);
     }
-    launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
     // two lanes per cell-level hide gather latency on small meshes; with a
     // million cell-levels or more there is parallelism enough, and the
     // second lane only idles through the per-cell tail on the FP64 pipe
-    if (nC >= (1 << 20))
+    const bool one_lane = nC >= (1 << 20);
+    if (!ocean) {
+      // sw: TB with B1 and TC with B2 as two fused launches, then B3
+      if (m.maxEoE == 10)
+        launch_pdl(k_adj_trb_b1<10>, nE, TPB, pdl, st, m, t, a, L);
+      else
+        launch_pdl(k_adj_trb_b1<0>, nE, TPB, pdl, st, m, t, a, L);
+      if (one_lane)
+        launch_pdl(k_adj_trc_b2<1>, nC + nV, TPB, pdl, st, m, t, a, L);
+      else
+        launch_pdl(k_adj_trc_b2<NLC>, nC * NLC + nV, TPB, pdl, st, m, t, a, L);
+      launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
+      return;
+    }
+    launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
+    if (one_lane)
       launch_pdl(k_adj_tr_c<1>, nC, TPB, pdl, st, m, t, L);
     else
       launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
-    a.lFt = A.lFt, a.lhet = A.lhet, a.muh_t = A.muh_t;
   }
   if (ocean) return;  // the ocean's h and u are prescribed: nothing more to reverse
   if (m.maxEoE == 10)
