@@ -229,12 +229,25 @@ def gpu_arm(args, cfg, extras=True):
     achieved = step_bytes / (ms_step * 1e-3) / 1e9
     traffic = None
     tkern = {}
+    traffic_scaled = None
     for k in model:
-        tfile = os.path.join(ROOT, "profiles", f"{k}_{args.config}.txt")
-        if os.path.exists(tfile):
+        # the capture of this workload, else one of the same kernel on a smaller
+        # mesh (same levels and tracers) scaled by the cells processed
+        for name in (args.config, args.config.replace("_l7", "_l6")):
+            tfile = os.path.join(ROOT, "profiles", f"{k}_{name}.txt")
+            if not os.path.exists(tfile):
+                continue
+            vals = {}
             for line in open(tfile):
-                if line.startswith("dram_bytes_per_launch:"):
-                    tkern[k] = float(line.split(":")[1])
+                if ":" in line and not line.startswith("#"):
+                    key, _, v = line.partition(":")
+                    vals[key.strip()] = v.split()[0] if v.split() else ""
+            if "dram_bytes_per_launch" in vals:
+                scale = mesh.nCells / float(vals.get("cells", mesh.nCells)) if name != args.config else 1.0
+                tkern[k] = float(vals["dram_bytes_per_launch"]) * scale
+                if name != args.config:
+                    traffic_scaled = f"ncu capture of {name} scaled by cells ({scale:.2f}x)"
+                break
     if len(tkern) == len(model):
         traffic = 4 * sum(tkern.values())
     top = max(prof, key=prof.get)
@@ -247,7 +260,8 @@ def gpu_arm(args, cfg, extras=True):
                               "(mpaso/perfmodel.py dataflow_bytes)",
                 "algorithmic_bytes_per_step": int(step_bytes),
                 "bytes_per_cell_update": round(step_bytes / units_rank, 1),
-                "traffic_note": "sum over the step's 12 launches of ncu dram__bytes_read + write (profiles/)",
+                "traffic_note": "sum over the step's 12 launches of ncu dram__bytes_read + write (profiles/)"
+                                + (f"; {traffic_scaled}" if traffic_scaled else ""),
                 "traffic_model": {"per_launch_bytes_per_step": int(model_bytes),
                                   "frac": round(model_bytes / (ms_step * 1e-3) / 1e9 / peak, 4),
                                   "note": "every array each launch touches, re-reads across the three "
@@ -813,6 +827,18 @@ def ensemble_arm(args):
         s.sync()
     t_serial = reduce_over_ranks(time.perf_counter() - t1, "max", device="cuda")
     n, ncells = len(specs), sum(cells)
+    # FP64 issue of the batch against the pipe's peak: the model's instructions
+    # per step of every member (mpaso/perfmodel.py) over the batch's step time
+    from mpaso.perfmodel import Dims, per_step, sw_kernels
+    fp64_step = sum(per_step(sw_kernels(Dims.of(mm, 1, 1, ff), True, True, True))[1]
+                    for mm, ff in zip(members, mfct))
+    pipe_peak = 2.0 * torch.cuda.get_device_properties(local).multi_processor_count * 2070e6
+    fp64_batch = {"instructions_per_step": int(fp64_step),
+                  "frac_of_pipe_peak": fp64_step * K / t_batch / pipe_peak,
+                  "ceiling_speedup_vs_serial": (t_serial / K) / (fp64_step / pipe_peak),
+                  "note": "FP64 thread instructions of all members' steps (model) over the batch time, against "
+                          "2 per clock per SM at 2070 MHz; ceiling = the serial time over the time the batch's "
+                          "FP64 work takes at the pipe's peak"}
     out = None
     if rank == 0:
         out = {"metric": "ensemble members*steps/s (one graph-captured launch sequence vs one at a time)",
@@ -838,6 +864,7 @@ def ensemble_arm(args):
                "one_at_a_time_serial": {"value": n * K / t_serial, "unit": "member-steps/s",
                                         "how": "members advanced strictly in turn (wait after each member)"},
                "speedup_vs_serial": t_serial / t_batch,
+               "fp64": fp64_batch,
                "setup": setup,
                "gpu_launches": st.launches_per_step() * K}
     for d, s in singles:
@@ -1046,7 +1073,7 @@ def extras_for_line(args):
     try:
         e = ensemble_arm(args)
         out["ensemble"] = {k: e[k] for k in ("value", "unit", "steps", "cell_updates_per_s", "persistent",
-                                             "one_at_a_time",
+                                             "fp64", "one_at_a_time",
                                              "speedup_vs_one_at_a_time", "one_at_a_time_serial",
                                              "speedup_vs_serial", "setup")}
         out["ensemble"]["workload"] = e["config"]["workload"]
