@@ -572,10 +572,17 @@ def adjoint_tracer_leg(args, mesh, N, K, dt):
               loss(*[a - eps * b for a, b in zip((h0, u0, tr0), v)])) / (2 * eps)
         ad = float(sum((g * x).sum() for g, x in zip((gh, gu, gt), v)))
         errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+    # the tracer part alone, over a short window, along directions away from the
+    # tracer's extrema (where the limiter keeps its branch)
+    fd_local = ocean_fd_away_from_extrema(st, mesh, tr0, trt, w, dt, min(args.adj_dirs, 8),
+                                          reset=((G.FIELD_H, h0), (G.FIELD_U, u0)))
     return {"workload": "same window, 1 tracer (FCT + del2 kappa=1e4), loss on the final tracer",
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
             "vjp_over_plain_forward": t_vjp / t_plain, "stored_window": stored,
-            "fd_check": {"directions": len(errs), "max_rel_err": max(errs) if errs else None},
+            "fd_check": {"directions": len(errs), "max_rel_err": max(errs) if errs else None,
+                         "note": "h, u and the tracer perturbed together over the whole 500-step window: "
+                                 "the FCT limiter changes branch within the perturbation"},
+            "fd_away_from_extrema": fd_local,
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
 
 
@@ -660,7 +667,7 @@ def ocean_adjoint_leg(args, N=20, K=10):
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
 
 
-def ocean_fd_away_from_extrema(st, mesh, tr0, trt, w, dt, ndirs, nsteps=2, rings=6):
+def ocean_fd_away_from_extrema(st, mesh, tr0, trt, w, dt, ndirs, nsteps=2, rings=6, reset=()):
     """Central differences of the forward against the adjoint over a short
     window (nsteps), along directions each supported on one cell and its
     neighbours, at one level and tracer, at least `rings` cells from every
@@ -690,11 +697,16 @@ def ocean_fd_away_from_extrema(st, mesh, tr0, trt, w, dt, ndirs, nsteps=2, rings
             front = cand
         return dist
 
-    def final(x):
+    def put(x):  # the tracers, and the fields a step advances with them (sw: h, u)
+        for fld, a in reset:
+            st.set(fld, a)
         st.set(G.FIELD_TRACERS, x)
+
+    def final(x):
+        put(x)
         st.step(dt, nsteps)
         return st.get(G.FIELD_TRACERS)
-    st.set(G.FIELD_TRACERS, tr0)
+    put(tr0)
     st.forward(dt, nsteps, 1)
     gN = w * (st.get(G.FIELD_TRACERS) - trt)
     gt = st.vjp_tracers(np.zeros((mesh.nCells, tr0.shape[1])), np.zeros((mesh.nEdges, tr0.shape[1])), gN)[2]
@@ -1051,7 +1063,7 @@ def extras_for_line(args):
             "fd_check": a["fd_check"], "peak_device_bytes": a["peak_device_bytes"],
             "stored_window": a["stored_window"],
             "with_tracer": {k: tr.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
-                                                   "peak_device_bytes")},
+                                                   "fd_away_from_extrema", "peak_device_bytes")},
             "ocean_tracers": {k: oc.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
                                                      "fd_away_from_extrema", "peak_device_bytes")}}
     except Exception as e:  # noqa: BLE001
@@ -1080,8 +1092,54 @@ def extras_for_line(args):
         out["ensemble"]["launch"] = e["config"]["launch"]
     except Exception as e:  # noqa: BLE001
         out["ensemble"] = {"error": repr(e)}
+    try:
+        out["threads_per_edge"] = lanes_table(args)
+    except Exception as e:  # noqa: BLE001
+        out["threads_per_edge"] = {"error": repr(e)}
     out["extras_wall_s"] = round(time.time() - t0, 1)
     return out
+
+
+def lanes_table(args, levels=(3, 4, 5, 7)):
+    """Time per RK4 step (sw + FCT tracer + del2) with 1, 2 and 4 threads per
+    edge-level in the TRiSK loop, the rest of the launch configuration as the
+    autotuner chose it, on spheres from too small to fill the GPU to the
+    benchmark's size; and the autotuner's own lane choice per mesh."""
+    import torch
+
+    import mpaso
+    import mpaso.gpu as G
+    from mpaso.initial import sw_state
+    from mpaso.setup import fct_statics
+    rows = []
+    for level in levels:
+        mesh = mpaso.Mesh.icosa(level)
+        dm = G.DeviceMesh(mesh, fct=fct_statics(mesh, 1))
+        st = G.State(dm, nlev=1, ntr=1, fct=True, hmix=True, kappa=1e4, nu=1e4)
+        h, u, tr = sw_state(mesh, 77, 1, 1)
+        for f, a in ((G.FIELD_H, h), (G.FIELD_U, u), (G.FIELD_TRACERS, tr)):
+            st.set(f, a)
+        dt = 60.0 * 2 ** (7 - level)
+        cfg = st.autotune(dt, 3)
+        ext = torch.cuda.ExternalStream(st.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = {}
+        n = max(20, 2000 >> max(level - 3, 0))
+        for lanes in (1, 2, 4):
+            st.set_launch_config(cfg["unroll"], cfg["threads"], cfg["capped"], cfg["l2"], cfg["overlap"],
+                                 cfg["split"], lanes)
+            st.step_graph(dt, 3)
+            st.sync()
+            e0.record(ext)
+            st.step_graph(dt, n)
+            e1.record(ext)
+            e1.synchronize()
+            ms[lanes] = e0.elapsed_time(e1) / n
+        rows.append({"level": level, "cells": mesh.nCells, "autotuned_lanes": cfg["lanes"],
+                     "ms_per_step": {str(k): round(v, 5) for k, v in ms.items()}})
+        st.close()
+        dm.close()
+    return rows
 
 
 def main():
