@@ -325,6 +325,7 @@ def gpu_arm(args, cfg, extras=True):
                    "copy in -> 1 step -> copy out every step)"
            if app == G.APP_SW else "mpaso_state_set/rk4_step_graph/state_get (C ABI, pinned host buffers)",
            "timing": f"median of repeated regions of {Ke} calls"}
+    e2e["host_link"] = host_link_rates(local)
     if app == G.APP_SW:
         bl = reduce_over_ranks(blocking_ms, "max", device="cuda")
         e2e["blocking"] = {"value": world * units_rank * Ke / (bl * 1e-3),
@@ -386,6 +387,45 @@ def gpu_arm(args, cfg, extras=True):
         }
     st.close()
     dm.close()
+    return out
+
+
+def host_link_rates(device, sizes_mb=(0.0625, 1, 6.5, 64, 256)):
+    """Copy rates between page-locked host memory and the device by transfer
+    size (one cudaMemcpyAsync each way, CUDA events, best of 5), and where the
+    page-locked buffers sit: the NUMA node of the host CPUs this process runs
+    on, next to the GPU's own node."""
+    import torch
+    out = {"unit": "GB/s", "h2d": {}, "d2h": {}}
+    st = torch.cuda.Stream(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for mb in sizes_mb:
+        n = int(mb * (1 << 20)) // 8
+        hb = torch.empty(n, dtype=torch.float64).pin_memory()
+        db = torch.empty(n, dtype=torch.float64, device=device)
+        for key, dst, src in (("h2d", db, hb), ("d2h", hb, db)):
+            best = 1e30
+            with torch.cuda.stream(st):
+                for _ in range(5):
+                    e0.record(st)
+                    dst.copy_(src, non_blocking=True)
+                    e1.record(st)
+                    e1.synchronize()
+                    best = min(best, e0.elapsed_time(e1))
+            out[key][f"{mb:g}MB"] = round(n * 8 / (best * 1e-3) / 1e9, 1)
+    try:
+        cpus = sorted(os.sched_getaffinity(0))
+        nodes = set()
+        for c in cpus:
+            for d in os.listdir(f"/sys/devices/system/cpu/cpu{c}"):
+                if d.startswith("node"):
+                    nodes.add(int(d[4:]))
+        out["host_cpu_numa_nodes"] = sorted(nodes)
+        bus = torch.cuda.get_device_properties(device).pci_bus_id if hasattr(
+            torch.cuda.get_device_properties(device), "pci_bus_id") else None
+        out["gpu_pci_bus_id"] = bus
+    except Exception as e:  # noqa: BLE001
+        out["numa"] = repr(e)
     return out
 
 
