@@ -1144,7 +1144,8 @@ def lanes_table(args, levels=(3, 4, 5, 7)):
     """Time per RK4 step (sw + FCT tracer + del2) with 1, 2 and 4 threads per
     edge-level in the TRiSK loop, the rest of the launch configuration as the
     autotuner chose it, on spheres from too small to fill the GPU to the
-    benchmark's size; and the autotuner's own lane choice per mesh."""
+    benchmark's size; the autotuner's own lane choice per mesh; and the same
+    steps as one persistent launch."""
     import torch
 
     import mpaso
@@ -1175,8 +1176,17 @@ def lanes_table(args, levels=(3, 4, 5, 7)):
             e1.record(ext)
             e1.synchronize()
             ms[lanes] = e0.elapsed_time(e1) / n
+        # the same steps in one persistent launch (autotuned launch shapes do not apply)
+        st.set_launch_config(cfg["unroll"], cfg["threads"], cfg["capped"], cfg["l2"], cfg["overlap"],
+                             cfg["split"], cfg["lanes"])
+        st.step_persistent(dt, 3)
+        e0.record(ext)
+        st.step_persistent(dt, n)
+        e1.record(ext)
+        e1.synchronize()
         rows.append({"level": level, "cells": mesh.nCells, "autotuned_lanes": cfg["lanes"],
-                     "ms_per_step": {str(k): round(v, 5) for k, v in ms.items()}})
+                     "ms_per_step": {str(k): round(v, 5) for k, v in ms.items()},
+                     "persistent_ms_per_step": round(e0.elapsed_time(e1) / n, 5)})
         st.close()
         dm.close()
     return rows
