@@ -305,22 +305,17 @@ __device__ __forceinline__ double combine(int rk, double dt, int64_t i, double m
 
 // B3 (cells + edges): thickness through kites; u through circulation, KE and
 // divergence; then the RK combination.
-__global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, int L) {
-  stage_prologue();
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t nCL = (int64_t)m.nC * L;
-  if (i < nCL) {
-    const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
-    double mh = a.mu_h[i];
-    for (int j = 0; j < m.maxEoC; ++j) {
-      const int64_t s = (int64_t)j * m.nC + c;
-      mh = fma(m.kiteR[s], a.lhs[(int64_t)m.vocR[s] * L + k], mh);
-    }
-    combine(a.rk, a.dt, i, mh, a.lam_h, a.acc_h, a.lk_h);
-    return;
+__device__ __forceinline__ void b3_cell_item(const DMesh &m, const AdjArgs &a, int L, int64_t i) {
+  const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
+  double mh = a.mu_h[i];
+  for (int j = 0; j < m.maxEoC; ++j) {
+    const int64_t s = (int64_t)j * m.nC + c;
+    mh = fma(m.kiteR[s], a.lhs[(int64_t)m.vocR[s] * L + k], mh);
   }
-  i -= nCL;
-  if (i >= (int64_t)m.nE * L) return;
+  combine(a.rk, a.dt, i, mh, a.lam_h, a.acc_h, a.lk_h);
+}
+
+__device__ __forceinline__ void b3_edge_item(const DMesh &m, const DStat &st, const AdjArgs &a, int L, int64_t i) {
   const int e = (int)(i / L), k = (int)(i - (int64_t)e * L);
   const int2 c = m.coe[e];
   const int2 v = m.voe[e];
@@ -334,6 +329,19 @@ __global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, in
   // the next stage's B1 inputs (B1 of this stage has completed)
   if (a.prep) prep_edge(m, a, L, e, k, i, a.un, a.hn, a.pvn, lk);
 }
+
+__global__ void __launch_bounds__(TPB) k_adj_b3(DMesh m, DStat st, AdjArgs a, int L) {
+  stage_prologue();
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (i < nCL) {
+    b3_cell_item(m, a, L, i);
+    return;
+  }
+  i -= nCL;
+  if (i < (int64_t)m.nE * L) b3_edge_item(m, st, a, L, i);
+}
+
 
 // ---------------------------------------------------------------------------
 // Tracer reverse, three launches per stage ahead of B1: TA (cells) the FCT
@@ -363,11 +371,8 @@ template <int NL> __device__ __forceinline__ double lane_sum(double v) {
 // slots; the bounds merge as (value, slot) with the lower slot (the cell
 // itself first) winning ties, which is the reference's sequential max / min.
 template <int NL, int NC>
-__global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tr_a_item(const DMesh &m, const TrArgs &a, int L, int64_t g) {
   const int lane = (int)(g & (NL - 1));
-  const int64_t nCL = (int64_t)m.nC * L;
-  if (g / NL >= nCL) return;  // whole groups: all lanes of a live cell stay
   const int64_t i = g / NL;
   const int c = (int)(i / L), k = (int)(i - (int64_t)c * L);
   const int n = m.nEoC[c], T = a.T;
@@ -462,6 +467,29 @@ __global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
   const double lhp = -lhpi * hpi * hpi;
   a.muh_t[i] = lh + lhp;
   a.lk_h[i] = fma(a.dt, lhp, a.lk_h[i]);
+}
+
+template <int NL, int NC>
+__global__ void __launch_bounds__(TPB) k_adj_tr_a(DMesh m, TrArgs a, int L) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g / NL >= (int64_t)m.nC * L) return;  // whole groups: all lanes of a live cell stay
+  tr_a_item<NL, NC>(m, a, L, g);
+}
+
+// B3 of this reversed stage with TA of the next one (the stage before it in the
+// forward, same segment): TA of a cell-level reads, of what B3 writes, only
+// the thickness-tendency cotangent of its own cell, so one thread does both.
+template <int NC>
+__global__ void __launch_bounds__(TPB) k_adj_b3_tra(DMesh m, DStat st, AdjArgs a, TrArgs tn, int L) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nCL = (int64_t)m.nC * L;
+  if (i < nCL) {
+    b3_cell_item(m, a, L, i);
+    tr_a_item<1, NC>(m, tn, L, i);
+    return;
+  }
+  i -= nCL;
+  if (i < (int64_t)m.nE * L) b3_edge_item(m, st, a, L, i);
 }
 
 // TB (edges): the cotangents of the stage's edge fluxes.  FCT: the limited
@@ -746,7 +774,30 @@ void ensure_buffers(SwState &s, int N, int k) {
 
 // Reverse of the stage whose input state is tape slot j; `first`: no B3 before
 // it prepared its edge quantities; `prep_next`: prepare those of slot j - 1.
-void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_next, cudaStream_t st) {
+// Tracer arguments of the reversed stage whose input state is tape slot j.
+TrArgs tr_args(SwState &s, AdjBuffers &A, int rk, int j) {
+  const DMesh &m = s.mesh->ctx.d;
+  const int64_t nE = (int64_t)m.nE * s.L, nC = (int64_t)m.nC * s.L;
+  const int64_t cT = nC * s.T, eT = nE * s.T;
+  TrArgs t{};
+  t.u = A.tp_u + (size_t)j * nE, t.h = A.tp_h + (size_t)j * nC, t.tr = A.tp_tr + (size_t)j * cT;
+  t.A = A.tp_A + (size_t)j * eT, t.LO = A.tp_LO + (size_t)j * eT, t.R2 = A.tp_R2 + (size_t)j * cT;
+  t.hpi = A.tp_hpi + (size_t)j * nC, t.tLO = A.tp_tLO + (size_t)j * cT;
+  if (s.p.app == MPASO_APP_OCEAN) {  // prescribed thickness, edge thickness, flux and 1/hProv
+    t.ocean = 1, t.h = s.H[0], t.hpi = s.HPI, t.Fx = s.F, t.hEx = s.HE;
+  }
+  t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.gq = A.gq, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
+  t.ltl = A.ltl, t.ltrs = A.ltrs, t.lfio = A.lfio, t.lmm = A.lmm, t.amm = A.amm;
+  t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.p12 = A.p12, t.lho = A.lho;
+  t.T = s.T, t.rk = rk, t.fct = s.p.fct ? 1 : 0, t.hmix = s.p.hmix ? 1 : 0, t.dt = A.dt;
+  t.centred = !t.fct && !t.ocean;
+  return t;
+}
+
+// `tra_done`: TA of this stage already ran with the previous reversed stage's
+// B3; returns whether this stage's B3 ran TA of the next one.
+bool stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_next, cudaStream_t st,
+               bool tra_done) {
   const DMesh &m = s.mesh->ctx.d;
   const int L = s.L;
   const int64_t nE = (int64_t)m.nE * L, nC = (int64_t)m.nC * L, nV = (int64_t)m.nV * L;
@@ -769,21 +820,9 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
   const bool ocean = s.p.app == MPASO_APP_OCEAN;
   if (first && !ocean) launch_pdl(k_adj_prep, nE, TPB, pdl, st, m, a, L);
   if (A.tr) {
-    const int64_t cT = nC * s.T, eT = nE * s.T;
-    TrArgs t{};
-    t.u = a.u, t.h = a.h, t.tr = A.tp_tr + (size_t)j * cT;
-    t.A = A.tp_A + (size_t)j * eT, t.LO = A.tp_LO + (size_t)j * eT, t.R2 = A.tp_R2 + (size_t)j * cT;
-    t.hpi = A.tp_hpi + (size_t)j * nC, t.tLO = A.tp_tLO + (size_t)j * cT;
-    if (ocean) {  // prescribed thickness, edge thickness, flux and 1/hProv
-      t.ocean = 1, t.h = s.H[0], t.hpi = s.HPI, t.Fx = s.F, t.hEx = s.HE;
-    }
-    t.kd = s.st.kd, t.lk_h = A.lk_h, t.lk_q = A.lk_q, t.gq = A.gq, t.lam_q = A.lam_q, t.acc_q = A.acc_q;
-    t.ltl = A.ltl, t.ltrs = A.ltrs, t.lfio = A.lfio, t.lmm = A.lmm, t.amm = A.amm;
-    t.muh_t = A.muh_t, t.lFt = A.lFt, t.lhet = A.lhet, t.p12 = A.p12, t.lho = A.lho;
-    t.T = s.T, t.rk = rk, t.fct = s.p.fct ? 1 : 0, t.hmix = s.p.hmix ? 1 : 0, t.dt = A.dt;
-    t.centred = !t.fct && !t.ocean;
+    const TrArgs t = tr_args(s, A, rk, j);
     constexpr int NLA = 1, NLC = 2;  // lanes per cell (measured best at level 6)
-    if (t.fct) {
+    if (t.fct && !tra_done) {
       if (m.maxEoC <= 6)
         launch_pdl(k_adj_tr_a<NLA, 6>, nC * NLA, TPB, pdl, st, m, t, L);
       else
@@ -803,8 +842,16 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
         launch_pdl(k_adj_trc_b2<1>, nC + nV, TPB, pdl, st, m, t, a, L);
       else
         launch_pdl(k_adj_trc_b2<NLC>, nC * NLC + nV, TPB, pdl, st, m, t, a, L);
+      if (t.fct && prep_next) {  // with TA of the next reversed stage (slot j - 1)
+        const TrArgs tn = tr_args(s, A, rk > 0 ? rk - 1 : 3, j - 1);
+        if (m.maxEoC <= 6)
+          launch_pdl(k_adj_b3_tra<6>, nC + nE, TPB, pdl, st, m, s.st, a, tn, L);
+        else
+          launch_pdl(k_adj_b3_tra<0>, nC + nE, TPB, pdl, st, m, s.st, a, tn, L);
+        return true;
+      }
       launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
-      return;
+      return false;
     }
     launch_pdl(k_adj_tr_b, nE, TPB, pdl, st, m, t, L);
     if (one_lane)
@@ -812,13 +859,14 @@ void stage_vjp(SwState &s, AdjBuffers &A, int rk, int j, bool first, bool prep_n
     else
       launch_pdl(k_adj_tr_c<NLC>, nC * NLC, TPB, pdl, st, m, t, L);
   }
-  if (ocean) return;  // the ocean's h and u are prescribed: nothing more to reverse
+  if (ocean) return false;  // the ocean's h and u are prescribed: nothing more to reverse
   if (m.maxEoE == 10)
     launch_pdl(k_adj_b1<10>, nE, TPB, pdl, st, m, a, L);
   else
     launch_pdl(k_adj_b1<0>, nE, TPB, pdl, st, m, a, L);
   launch_pdl(k_adj_b2, nC + nV, TPB, pdl, st, m, a, L);
   launch_pdl(k_adj_b3, nC + nE, TPB, pdl, st, m, s.st, a, L);
+  return false;
 }
 
 void tape_segment(SwState &s, AdjBuffers &A, int n, bool with_tr, cudaStream_t st);
@@ -1000,10 +1048,11 @@ void reverse_body(SwState &s) {
       if (A.tr)
         k_adj_init_q<<<blocks_for(cT, TPB), TPB, 0, st>>>(m, s.L, s.T, A.lam_q, A.lk_q, A.gq, A.dt / 6);
     }
+    bool tra_done = false;  // TA of the next reversed stage already ran with B3
     for (int t = n - 1; t >= 0; --t)
       for (int rk = 3; rk >= 0; --rk) {
         const int j = 4 * t + rk;
-        stage_vjp(s, A, rk, j, t == n - 1 && rk == 3, j > 0, st);
+        tra_done = stage_vjp(s, A, rk, j, t == n - 1 && rk == 3, j > 0, st, tra_done);
       }
   }
   // q = h tr at the window's start (tape slot 0 holds checkpoint 0)
