@@ -82,7 +82,11 @@ struct AdjBuffers {
   // the whole reverse sweep, captured once per (N, k, dt, tracers) and replayed
   cudaGraphExec_t rev = nullptr;
   int rev_N = 0, rev_k = 0, rev_tr = 0;
-  bool rev_stored = false;
+  bool rev_stored = false, rev_skip = false;
+  // the checkpointing forward taped its last segment (tracers taped: last_tr);
+  // the reverse sweep then starts without recomputing that segment
+  bool last_taped = false;
+  int last_tr = 0;
   double rev_dt = 0.0;
   int tr = 0;  // the sweep being run reverses the tracers too
   // ckpt_every = 0: the forward tapes the whole window (one segment), the
@@ -917,6 +921,7 @@ void forward_stored(SwState &s, double dt, int N) {
 }
 
 void forward(SwState &s, double dt, int N, int k) {
+  void tape_segment(SwState &, AdjBuffers &, int, bool, cudaStream_t);
   const bool ocean = s.p.app == MPASO_APP_OCEAN;
   require(!ocean || s.T > 0, MPASO_ERR_ARG, "the ocean app's adjoint differentiates its tracers: ntr >= 1");
   require(!s.p.pin_u, MPASO_ERR_ARG, "the adjoint does not support a pinned wind (test case 1)");
@@ -941,9 +946,36 @@ void forward(SwState &s, double dt, int N, int k) {
   }
   const size_t ct = ch * s.T;
   if (s.T) MPASO_CUDA(cudaMemcpyAsync(A.ck_tr, s.TR0, ct, cudaMemcpyDeviceToDevice, s.stream));
+  A.last_taped = false;
   for (int done = 0, c = 1; done < N; ++c) {
     const int n = std::min(k, N - done);
-    sw_steps_graph(s, dt, n);
+    if (done + n < N) {
+      sw_steps_graph(s, dt, n);
+    } else {
+      // the last segment with its tape, which the reverse sweep needs first:
+      // from the state through tape slots 0..4n, and the final state back
+      const bool tr = s.T > 0;
+      const size_t cb = ct;
+      if (ocean) ocean_prepare(s, dt, s.stream);
+      if (!ocean) {
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_u, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
+        MPASO_CUDA(cudaMemcpyAsync(A.tp_h, s.H[0], ch, cudaMemcpyDeviceToDevice, s.stream));
+      }
+      if (tr) MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, s.TR0, cb, cudaMemcpyDeviceToDevice, s.stream));
+      tape_segment(s, A, n, tr, s.stream);
+      if (!ocean) {
+        MPASO_CUDA(cudaMemcpyAsync(s.U[0], A.tp_u + (size_t)4 * n * m.nE * s.L, eu, cudaMemcpyDeviceToDevice,
+                                   s.stream));
+        MPASO_CUDA(cudaMemcpyAsync(s.H[0], A.tp_h + (size_t)4 * n * m.nC * s.L, ch, cudaMemcpyDeviceToDevice,
+                                   s.stream));
+      }
+      if (tr)
+        MPASO_CUDA(cudaMemcpyAsync(s.TR0, A.tp_tr + (size_t)4 * n * m.nC * s.L * s.T, cb,
+                                   cudaMemcpyDeviceToDevice, s.stream));
+      MPASO_CUDA(cudaGetLastError());
+      s.diag_valid = false;  // the state's diagnostics buffers held the tape's stages
+      A.last_taped = true, A.last_tr = tr ? 1 : 0;
+    }
     done += n;
     if (done < N && !ocean) {
       MPASO_CUDA(cudaMemcpyAsync(A.ck_u + (size_t)c * m.nE * s.L, s.U[0], eu, cudaMemcpyDeviceToDevice, s.stream));
@@ -1025,7 +1057,7 @@ void reverse_body(SwState &s) {
   if (ocean) ocean_recompute(s, A.dt, st);  // the prescribed flux and 1/hProv the stages used
   for (int seg = A.nck - 1; seg >= 0; --seg) {
     const int s0 = seg * A.k, n = std::min(A.k, A.N - s0);
-    if (!A.stored) {
+    if (!A.stored && !(seg == A.nck - 1 && A.rev_skip)) {
       // taping recompute of the segment from its checkpoint
       if (!ocean) {
         MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
@@ -1065,11 +1097,17 @@ void reverse_body(SwState &s) {
 // once as a graph for the current (N, k, dt) and buffers, then replayed.
 void reverse(SwState &s) {
   AdjBuffers &A = *s.adj;
-  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt || A.rev_tr != A.tr || A.rev_stored != A.stored)) {
+  // the forward's tape of the last segment serves one reverse sweep of the same
+  // tracer mode (the sweep's recomputes overwrite it)
+  const bool skip = !A.stored && A.last_taped && A.last_tr == (A.tr ? 1 : 0);
+  A.last_taped = false;
+  if (A.rev && (A.rev_N != A.N || A.rev_k != A.k || A.rev_dt != A.dt || A.rev_tr != A.tr ||
+                A.rev_stored != A.stored || A.rev_skip != skip)) {
     cudaGraphExecDestroy(A.rev);
     A.rev = nullptr;
   }
   if (!A.rev) {
+    A.rev_skip = skip;  // read by reverse_body
     cudaGraph_t g;
     MPASO_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
     try {

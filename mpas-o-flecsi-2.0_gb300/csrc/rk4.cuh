@@ -218,6 +218,7 @@ void sw_launch_stage(SwState &s, const Stage &S, cudaStream_t st);
 Stage ocean_make_stage(SwState &s, int rk, double dt);
 void ocean_launch_stage(SwState &s, const Stage &S, cudaStream_t st);
 void ocean_recompute(SwState &s, double dt, cudaStream_t st);
+void ocean_prepare(SwState &s, double dt, cudaStream_t st);
 void drop_adjoint_graph(SwState &s);
 
 // ---------------------------------------------------------------------------
