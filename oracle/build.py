@@ -11,6 +11,7 @@
 Usage: python oracle/build.py [--force]
 """
 import os
+import re
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -88,39 +89,113 @@ def build_ref(force=False):
         return out
 
 
+_INCLUDE = re.compile(r'^\s*#\s*include\s*([<"])([^>"]+)[>"]')
+_ONCE = re.compile(r"^\s*#\s*pragma\s+once\b")
+
+
+def amalgamate(src, dirs, label):
+    """Text of the translation unit `src` with every #include that resolves in
+    `dirs` (a quoted one first beside the including file, as the compiler looks)
+    replaced by the included file's text, recursively; headers found nowhere in
+    `dirs` (the system's) stay #include lines.  A header with #pragma once is
+    inlined once; #line directives keep diagnostics pointing at the sources.
+    `label(path)` names a file in those directives."""
+    once, out = set(), []
+
+    def emit(path):
+        with open(path) as f:
+            text = f.read().splitlines()
+        if any(_ONCE.match(x) for x in text):
+            real = os.path.realpath(path)
+            if real in once:
+                return
+            once.add(real)
+        out.append(f'#line 1 "{label(path)}"')
+        for n, line in enumerate(text, 1):
+            if _ONCE.match(line):
+                out.append("")
+                continue
+            m = _INCLUDE.match(line)
+            if m:
+                look = ([os.path.dirname(path)] if m.group(1) == '"' else []) + list(dirs)
+                hit = next((os.path.join(d, m.group(2)) for d in look if os.path.isfile(os.path.join(d, m.group(2)))),
+                           None)
+                if hit:
+                    emit(hit)
+                    out.append(f'#line {n + 1} "{label(path)}"')
+                    continue
+            out.append(line)
+
+    emit(src)
+    return "\n".join(out) + "\n"
+
+
+FLW_DIR = os.path.join(HERE, "_ref", "flw")  # the wrapper build's translation units, amalgamated
+FLW_UNITS = ["init_functions.cc", "ref_driver.cc", "flecsi_probe.cc", "sw_tasks.cc", "ocean_tasks.cc"]
+
+
+def _write_if_changed(path, text):
+    if os.path.exists(path):
+        with open(path) as f:
+            if f.read() == text:
+                return
+    with open(path, "w") as f:
+        f.write(text)
+
+
 def build_flecsi_wrappers(force=False):
     """oracle/_ref/libref_gb300_L1_T1.so: the reference's own driver logic
     (ref_driver.cc) and FCT setup (init_functions.cc) with the FleCSI wrapper
     library's task bodies (mpas-o-flecsi-2.0_gb300/flecsi/) in place of the
     reference's apps/sw/tasks/solve.cc and apps/ocean/tasks/solve.cc, linked
     against libmpaso: it links only if every task the driver calls is defined
-    with the reference's declared signature.  None without a checkout."""
-    if not ref_available():
-        return None
+    with the reference's declared signature.
+
+    Two steps.  Where the reference checkout is present, each translation unit
+    is amalgamated (its reference, shim and wrapper headers inlined) into
+    oracle/_ref/flw/, a git-ignored build output like the libraries.  The
+    units are then compiled from there, so a host without the checkout (the
+    GPU host) builds the library from the units made beside one.  None when
+    neither the checkout nor the units are there."""
     pkg = os.path.join(os.path.dirname(HERE), "mpas-o-flecsi-2.0_gb300")
     wrap = os.path.join(pkg, "flecsi")
     lib_dir = os.path.join(pkg, "lib")
     out_dir = os.path.join(HERE, "_ref")
-    os.makedirs(out_dir, exist_ok=True)
-    shim = os.path.join(HERE, "shim")
-    srcs = [os.path.join(REF, "apps/ocean/tasks/init_functions.cc"), os.path.join(HERE, "ref_driver.cc"),
-            os.path.join(HERE, "flecsi_probe.cc"), os.path.join(wrap, "sw_tasks.cc"),
-            os.path.join(wrap, "ocean_tasks.cc")]
-    deps = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs] + srcs + [
-        os.path.join(wrap, "mpaso_flecsi.hh"), os.path.join(HERE, "build.py"), os.path.join(HERE, "sw_extra.c"),
-        os.path.join(os.path.dirname(HERE), "include", "mpaso.h")]
+    root = os.path.dirname(HERE)
+    if ref_available():
+        os.makedirs(FLW_DIR, exist_ok=True)
+        srcs = [os.path.join(REF, "apps/ocean/tasks/init_functions.cc"), os.path.join(HERE, "ref_driver.cc"),
+                os.path.join(HERE, "flecsi_probe.cc"), os.path.join(wrap, "sw_tasks.cc"),
+                os.path.join(wrap, "ocean_tasks.cc")]
+        dirs = [os.path.join(HERE, "shim"), REF, HERE, wrap, os.path.join(root, "include")]
+
+        def label(p):
+            p = os.path.realpath(p)
+            for base, name in ((os.path.realpath(REF), "reference"), (os.path.realpath(root), ".")):
+                if p.startswith(base + os.sep):
+                    return os.path.join(name, os.path.relpath(p, base))
+            return os.path.basename(p)
+
+        for name, src in zip(FLW_UNITS, srcs):
+            _write_if_changed(os.path.join(FLW_DIR, name), amalgamate(src, dirs, label))
+    units = [os.path.join(FLW_DIR, n) for n in FLW_UNITS]
+    if not all(os.path.exists(u) for u in units):
+        return None
+    extra = os.path.join(HERE, "sw_extra.c")
     out = os.path.join(out_dir, "libref_gb300_L1_T1.so")
-    if not (force or _stale(out, deps)):
+    if not (force or _stale(out, units + [extra, os.path.join(HERE, "build.py")])):
         return out
     defs = ["-DMPASO_REF_NVL=1", "-DMPASO_REF_NTR=1", f"-DMPASO_REF_GRAVITY={GRAVITY}"]
-    inc = [f"-I{shim}", f"-I{REF}", f"-I{HERE}", f"-I{wrap}", f"-I{os.path.join(os.path.dirname(HERE), 'include')}"]
-    objs = []
-    for src in srcs:
-        obj = os.path.join(out_dir, "gb300_" + os.path.basename(src) + ".o")
-        _run(["g++", "-std=c++17", *CFLAGS, *defs, *inc, "-w", "-c", src, "-o", obj])
-        objs.append(obj)
+
+    def compile_unit(u):
+        obj = os.path.join(out_dir, "gb300_" + os.path.basename(u) + ".o")
+        _run(["g++", "-std=c++17", *CFLAGS, *defs, "-w", "-c", u, "-o", obj])
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        objs = list(ex.map(compile_unit, units))
     obj = os.path.join(out_dir, "gb300_sw_extra.o")
-    _run(["gcc", "-std=c11", *CFLAGS, f"-I{HERE}", "-c", os.path.join(HERE, "sw_extra.c"), "-o", obj])
+    _run(["gcc", "-std=c11", *CFLAGS, f"-I{HERE}", "-c", extra, "-o", obj])
     objs.append(obj)
     _run(["g++", "-shared", "-o", out, *objs, f"-L{lib_dir}", "-lmpaso", f"-Wl,-rpath,{lib_dir}", "-lm"])
     return out

@@ -9,9 +9,11 @@
 
 namespace flecsi {
 
-// One process, one color (the specialization makes one color per process,
-// mpasoflecsi/specialization/mesh.cc:31).
-inline std::size_t processes() { return 1; }
+// Processes, i.e. colors (the specialization makes one color per process,
+// mpasoflecsi/specialization/mesh.cc:31).  One in every oracle run; a test
+// probe sets more to check the wrappers' refusal of multi-color runs.
+inline std::size_t process_count = 1;
+inline std::size_t processes() { return process_count; }
 
 struct option_default_t {};
 inline constexpr option_default_t option_default{};

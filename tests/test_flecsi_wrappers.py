@@ -4,7 +4,8 @@ apps/ocean/tasks/solve.cc in a build of the reference's own driver logic
 through the header shim.  The build links only if every task the driver calls
 is defined with the signature the reference declares; the calls then reach
 libmpaso (on a host without a GPU they stop at its no-device error).  Needs
-the reference checkout, so it runs where the oracle builds (not on GPU hosts)."""
+the reference checkout, so it runs where the oracle builds; the library's
+runs on a GPU are in test_gpu_flecsi_wrappers.py."""
 import ctypes
 import runpy
 import os
@@ -44,13 +45,31 @@ def test_wrappers_reach_libmpaso(wrapped):
     m = mpaso.Mesh.icosa(2)
     om, st = S.mesh(m), S.static(m)
     err = ctypes.create_string_buffer(512)
-    rc = wrapped.flw_make_context(ctypes.byref(om), ctypes.byref(st), err, 512)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    xyz = np.concatenate([m.fields[k] for k in ("xCell", "yCell", "zCell")])
+    rc = wrapped.flw_make_context(ctypes.byref(om), ctypes.byref(st), p(xyz), 0, err, 512)
     from mpaso.gpu import device_count
     if device_count() == 0:
         assert rc == 1 and "mpaso_mesh_create" in err.value.decode()
     h, u, tr = sw_state(m, 1, 1, 1)
-    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
     if rc != 0:  # the reference driver through the wrappers, without a context
         rc2 = wrapped.orc_sw_run(ctypes.byref(om), ctypes.byref(st), ctypes.byref(S.config(1, 1)),
                                  ctypes.c_double(300.0), 1, p(h), p(u), p(tr))
         assert rc2 == 1 and "make_mesh_context" in wrapped.orc_last_error().decode()
+
+
+def test_wrappers_refuse_multi_color_runs(wrapped):
+    """More than one color (process) is refused before any device work: the
+    device mesh context has no halo exchange."""
+    S = Oracle("restatement")
+    m = mpaso.Mesh.icosa(2)
+    om, st = S.mesh(m), S.static(m)
+    err = ctypes.create_string_buffer(512)
+    xyz = np.concatenate([m.fields[k] for k in ("xCell", "yCell", "zCell")])
+    wrapped.flw_set_processes(2)
+    try:
+        rc = wrapped.flw_make_context(ctypes.byref(om), ctypes.byref(st), xyz.ctypes.data_as(ctypes.c_void_p), 0,
+                                      err, 512)
+    finally:
+        wrapped.flw_set_processes(1)
+    assert rc == 1 and "single-color" in err.value.decode()
