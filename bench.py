@@ -703,6 +703,10 @@ def ocean_adjoint_leg(args, N=20, K=10):
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
             "vjp_over_plain_forward": t_vjp / t_plain,
             "fd_check": fd_rows, "fd_away_from_extrema": fd_local,
+            "fd_note": "fd_check perturbs every cell over the whole window: near tracer extrema the perturbation "
+                       "moves the FCT limiter across its branches (the loss is not differentiable there), so those "
+                       "quotients need not converge to the adjoint; fd_away_from_extrema keeps the limiter on one "
+                       "branch and is the check of record",
             "adjoint_device_bytes": int(st.adjoint_device_bytes()),
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
 
@@ -1105,7 +1109,7 @@ def extras_for_line(args):
             "with_tracer": {k: tr.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
                                                    "fd_away_from_extrema", "peak_device_bytes")},
             "ocean_tracers": {k: oc.get(k) for k in ("workload", "ratio", "vjp_over_plain_forward", "fd_check",
-                                                     "fd_away_from_extrema", "peak_device_bytes")}}
+                                                     "fd_away_from_extrema", "fd_note", "peak_device_bytes")}}
     except Exception as e:  # noqa: BLE001
         out["adjoint"] = {"error": repr(e)}
     log(f"extras: adjoint done at {time.time() - t0:.0f}s")
