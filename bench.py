@@ -620,7 +620,7 @@ def adjoint_tracer_leg(args, mesh, N, K, dt):
             "forward_ms": t_fwd, "forward_plain_ms": t_plain, "vjp_ms": t_vjp, "ratio": t_vjp / t_fwd,
             "vjp_over_plain_forward": t_vjp / t_plain, "stored_window": stored,
             "fd_check": {"directions": len(errs), "max_rel_err": max(errs) if errs else None,
-                         "note": "h, u and the tracer perturbed together over the whole 500-step window: "
+                         "note": f"h, u and the tracer perturbed together over the whole {N}-step window: "
                                  "the FCT limiter changes branch within the perturbation"},
             "fd_away_from_extrema": fd_local,
             "peak_device_bytes": int(dm.device_bytes() + st.device_bytes() + st.adjoint_device_bytes())}
