@@ -242,7 +242,9 @@ int mpaso_state_check_finite(mpaso_state s);
 int mpaso_rk4_step(mpaso_state s, double dt, int32_t nsteps);
 /* Same, replayed from a CUDA graph of one step (captured on first use for dt). */
 int mpaso_rk4_step_graph(mpaso_state s, double dt, int32_t nsteps);
-/* One call through the boundary with host buffers: copy in, nsteps, copy out. */
+/* One call through the boundary with host buffers: copy in, nsteps, copy out.
+ * Mapped page-locked buffers are read and written in place by the exchange's
+ * kernels (one pass per field each way); other buffers are staged. */
 int mpaso_rk4_step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u,
                         double *tracers);
 /* The same exchange queued on the state's stream without waiting for it

@@ -92,6 +92,7 @@ struct MeshCtx {
   std::vector<int32_t> perm[3];   // new -> reference id
   std::vector<int32_t> iperm[3];  // reference id -> new
   int32_t *d_perm[3] = {nullptr, nullptr, nullptr};  // device copies of perm
+  int32_t *d_iperm[3] = {nullptr, nullptr, nullptr};  // device copies of iperm
   void *arena = nullptr;
   size_t arena_bytes = 0;
   // growable scratch for the per-task entries

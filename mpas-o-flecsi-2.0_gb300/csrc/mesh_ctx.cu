@@ -17,6 +17,8 @@ MeshCtx::~MeshCtx() {
   if (geo) cudaFree(geo);
   for (auto &p : d_perm)
     if (p) cudaFree(p);
+  for (auto &p : d_iperm)
+    if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -475,6 +477,8 @@ void build(MeshCtx &ctx, const mpaso_mesh_desc &d, const std::vector<int64_t> *m
     const size_t bytes = ctx.perm[t].size() * sizeof(int32_t);
     MPASO_CUDA(cudaMalloc(&ctx.d_perm[t], bytes));
     MPASO_CUDA(cudaMemcpy(ctx.d_perm[t], ctx.perm[t].data(), bytes, cudaMemcpyHostToDevice));
+    MPASO_CUDA(cudaMalloc(&ctx.d_iperm[t], bytes));
+    MPASO_CUDA(cudaMemcpy(ctx.d_iperm[t], ctx.iperm[t].data(), bytes, cudaMemcpyHostToDevice));
   }
 }
 
@@ -735,7 +739,9 @@ int mpaso_mesh_set_gravity(mpaso_mesh m, double gravity) {
 int mpaso_mesh_device_bytes(mpaso_mesh m, int64_t *bytes) {
   return mpaso::guarded("mpaso_mesh_device_bytes", [&] {
     mpaso::require(m && bytes, MPASO_ERR_ARG, "null argument");
-    *bytes = (int64_t)(m->ctx.arena_bytes + m->ctx.scratch_bytes);
+    const mpaso::DMesh &d = m->ctx.d;
+    // the arena, the per-task scratch and both permutations of each entity
+    *bytes = (int64_t)(m->ctx.arena_bytes + m->ctx.scratch_bytes) + 2 * 4 * (d.nC + d.nE + d.nV);
   });
 }
 

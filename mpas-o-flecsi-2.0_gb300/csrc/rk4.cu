@@ -1254,11 +1254,20 @@ void step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u, d
     double *dh = ensure_io(S, bytes), *du = dh + nh, *dtr = du + nu;
     // Page-locked buffers: the whole exchange (copies in, permutations, steps,
     // copies out) is one graph, captured once per buffer set, dt and nsteps.
-    bool locked = true;
-    for (const void *p : {(const void *)h, (const void *)u, (const void *)(tr ? tracers : h)}) {
-      cudaPointerAttributes a;
-      if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) locked = false;
-      cudaGetLastError();
+    // Page-locked buffers mapped into the device's address space (the usual
+    // case) also get device aliases: the exchange kernels then move and
+    // permute each field in one pass over the host link.
+    bool locked = true, mapped = true;
+    double *alias[3] = {nullptr, nullptr, nullptr};
+    {
+      const void *ptrs[3] = {h, u, tr ? tracers : h};
+      for (int f = 0; f < 3; ++f) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, ptrs[f]) != cudaSuccess || a.type != cudaMemoryTypeHost) locked = false;
+        else alias[f] = (double *)a.devicePointer;
+        cudaGetLastError();
+        mapped = mapped && alias[f] != nullptr;
+      }
     }
     require(wait || locked, MPASO_ERR_ARG, "the asynchronous exchange needs page-locked host buffers");
     const XKey key{h, u, tr ? tracers : nullptr, dt, nsteps};
@@ -1276,10 +1285,10 @@ void step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u, d
       for (auto &e : S.x_ev) MPASO_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     if (locked) MPASO_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    // one copy per field each way (copy engines; page-locked buffers go at link speed),
-    // the permutations on the device, one synchronisation.  (Letting the permutation
-    // kernels read and write mapped host memory directly was slower: their accesses
-    // are scattered.)
+    // Pageable buffers: one copy per field each way through the staging
+    // buffer and the permutation kernels.  Page-locked ones: see above (a
+    // kernel that gathered from mapped host memory in context order was slower
+    // than the copy engines; walking the host side in its own order is not).
     try {
     if (!locked) {
       MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1305,17 +1314,28 @@ void step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u, d
       // kernel, and the tracers after it.
       const cudaStream_t su = S.x_side[0], sx = S.x_side[1];
       cudaEvent_t *E = S.x_ev;
+      const int32_t *ic = ctx.d_iperm[MPASO_CELLS], *ie = ctx.d_iperm[MPASO_EDGES];
       MPASO_CUDA(cudaEventRecord(E[0], st));
       MPASO_CUDA(cudaStreamWaitEvent(su, E[0], 0));
       MPASO_CUDA(cudaStreamWaitEvent(sx, E[0], 0));
-      MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
-      k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
-      MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, su));
-      k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
-      MPASO_CUDA(cudaEventRecord(E[1], su));
-      if (tr) {
-        MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, sx));
-        k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
+      if (mapped) {  // one pass per field; the tracers after h and u, under the diagnostics
+        host_rows_pub(true, alias[0], S.H[0], ic, nC, (int)L, ctx.sms, st);
+        host_rows_pub(true, alias[1], S.U[0], ie, nE, (int)L, ctx.sms, su);
+        MPASO_CUDA(cudaEventRecord(E[1], su));
+        if (tr) {
+          MPASO_CUDA(cudaStreamWaitEvent(sx, E[1], 0));
+          host_rows_pub(true, alias[2], S.TR0, ic, nC, (int)(L * S.T), ctx.sms, sx);
+        }
+      } else {
+        MPASO_CUDA(cudaMemcpyAsync(dh, h, nh * sizeof(double), cudaMemcpyHostToDevice, st));
+        k_gather_rows_pub(dh, S.H[0], ctx.d_perm[MPASO_CELLS], nC, (int)L, st);
+        MPASO_CUDA(cudaMemcpyAsync(du, u, nu * sizeof(double), cudaMemcpyHostToDevice, su));
+        k_gather_rows_pub(du, S.U[0], ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
+        MPASO_CUDA(cudaEventRecord(E[1], su));
+        if (tr) {
+          MPASO_CUDA(cudaMemcpyAsync(dtr, tracers, nt * sizeof(double), cudaMemcpyHostToDevice, sx));
+          k_gather_rows_pub(dtr, S.TR0, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
+        }
       }
       MPASO_CUDA(cudaEventRecord(E[2], sx));
       MPASO_CUDA(cudaStreamWaitEvent(st, E[1], 0));
@@ -1340,17 +1360,26 @@ void step_host(mpaso_state s, double dt, int32_t nsteps, double *h, double *u, d
       }
       MPASO_CUDA(cudaEventRecord(E[5], st));
       MPASO_CUDA(cudaStreamWaitEvent(su, E[3], 0));
-      k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
-      MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, su));
-      MPASO_CUDA(cudaEventRecord(E[4], su));
       MPASO_CUDA(cudaStreamWaitEvent(sx, E[3], 0));
-      k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, sx);
-      MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, sx));
-      if (tr) {
-        MPASO_CUDA(cudaStreamWaitEvent(sx, E[5], 0));
-        k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
-        MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, sx));
+      if (mapped) {
+        host_rows_pub(false, S.U[0], alias[1], ie, nE, (int)L, ctx.sms, su);
+        host_rows_pub(false, S.H[0], alias[0], ic, nC, (int)L, ctx.sms, sx);
+        if (tr) {
+          MPASO_CUDA(cudaStreamWaitEvent(sx, E[5], 0));
+          host_rows_pub(false, S.TR0, alias[2], ic, nC, (int)(L * S.T), ctx.sms, sx);
+        }
+      } else {
+        k_scatter_rows_pub(S.U[0], du, ctx.d_perm[MPASO_EDGES], nE, (int)L, su);
+        MPASO_CUDA(cudaMemcpyAsync(u, du, nu * sizeof(double), cudaMemcpyDeviceToHost, su));
+        k_scatter_rows_pub(S.H[0], dh, ctx.d_perm[MPASO_CELLS], nC, (int)L, sx);
+        MPASO_CUDA(cudaMemcpyAsync(h, dh, nh * sizeof(double), cudaMemcpyDeviceToHost, sx));
+        if (tr) {
+          MPASO_CUDA(cudaStreamWaitEvent(sx, E[5], 0));
+          k_scatter_rows_pub(S.TR0, dtr, ctx.d_perm[MPASO_CELLS], nC, (int)(L * S.T), sx);
+          MPASO_CUDA(cudaMemcpyAsync(tracers, dtr, nt * sizeof(double), cudaMemcpyDeviceToHost, sx));
+        }
       }
+      MPASO_CUDA(cudaEventRecord(E[4], su));
       MPASO_CUDA(cudaEventRecord(E[6], sx));
       MPASO_CUDA(cudaStreamWaitEvent(st, E[4], 0));  // join the side streams before the capture ends
       MPASO_CUDA(cudaStreamWaitEvent(st, E[6], 0));

@@ -20,6 +20,56 @@ __global__ void k_scatter_rows(const double *__restrict__ src, double *__restric
   dst[(int64_t)perm[e] * row + r] = src[i];
 }
 
+// Rows between page-locked host memory (reference order, read or written
+// through its device alias) and device memory (context order), in one pass:
+// the host side is walked in order, 16 bytes a thread where both sides allow
+// (coalesced over the host link), and the device side is scattered through
+// iperm (reference id -> context id).  import: dst[iperm[j]] = src[j];
+// export: dst[j] = src[iperm[j]] (rows of `row` doubles).
+template <bool IMPORT>
+__global__ void k_host_rows(const double *__restrict__ src, double *__restrict__ dst,
+                            const int32_t *__restrict__ iperm, int64_t n, int row, bool pairs) {
+  const int64_t total = n * row, stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  auto dev = [&](int64_t i) {
+    const int64_t j = i / row, r = i - j * row;
+    return (int64_t)iperm[j] * row + r;
+  };
+  if (pairs) {  // total even, host side 16-byte aligned
+    for (int64_t p = t0; p < total / 2; p += stride) {
+      const int64_t i = 2 * p;
+      if constexpr (IMPORT) {
+        const double2 v = reinterpret_cast<const double2 *>(src)[p];
+        dst[dev(i)] = v.x;
+        dst[dev(i + 1)] = v.y;
+      } else {
+        reinterpret_cast<double2 *>(dst)[p] = make_double2(src[dev(i)], src[dev(i + 1)]);
+      }
+    }
+  } else {
+    for (int64_t i = t0; i < total; i += stride) {
+      if constexpr (IMPORT)
+        dst[dev(i)] = src[i];
+      else
+        dst[i] = src[dev(i)];
+    }
+  }
+}
+
+void host_rows_pub(bool import, const double *src, double *dst, const int32_t *iperm, int64_t n, int row,
+                   int sms, cudaStream_t s) {
+  const int64_t total = n * row;
+  const double *host = import ? src : dst;
+  const bool pairs = total % 2 == 0 && ((uintptr_t)host & 15) == 0;
+  const int64_t work = pairs ? total / 2 : total;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(blocks_for(work, 256), (int64_t)sms * 8));
+  if (import)
+    k_host_rows<true><<<blocks, 256, 0, s>>>(src, dst, iperm, n, row, pairs);
+  else
+    k_host_rows<false><<<blocks, 256, 0, s>>>(src, dst, iperm, n, row, pairs);
+  MPASO_CUDA(cudaGetLastError());
+}
+
 void k_gather_rows_pub(const double *src, double *dst, const int32_t *perm, int64_t n, int row,
                        cudaStream_t s) {
   k_gather_rows<<<blocks_for(n * row, 256), 256, 0, s>>>(src, dst, perm, n, row);

@@ -13,6 +13,11 @@ __global__ void k_scatter_rows(const double *__restrict__ src, double *__restric
                                const int32_t *__restrict__ perm, int64_t n, int row);
 
 bool is_device_pointer(const void *p);
+// One pass between a page-locked host array (reference order, through its
+// device alias) and a device array (context order): import (host -> device)
+// or export; iperm maps reference ids to context ids.
+void host_rows_pub(bool import, const double *src, double *dst, const int32_t *iperm, int64_t n, int row,
+                   int sms, cudaStream_t s);
 void k_gather_rows_pub(const double *src, double *dst, const int32_t *perm, int64_t n, int row,
                        cudaStream_t s);
 void k_scatter_rows_pub(const double *src, double *dst, const int32_t *perm, int64_t n, int row,

@@ -180,6 +180,41 @@ def test_host_boundary_call_with_page_locked_buffers():
     assert np.array_equal(hp.numpy(), h) and np.array_equal(up.numpy(), u) and np.array_equal(tp.numpy(), tr)
 
 
+@pytest.mark.parametrize("offset", [0, 1])
+def test_page_locked_exchange_odd_sizes_and_unaligned_buffers(offset):
+    """The one-pass exchange of mapped page-locked buffers (16-byte host accesses
+    where the field's size and the buffer's alignment allow, 8-byte ones
+    otherwise) equals the staged path of pageable buffers bit for bit, with
+    buffers on a 16-byte boundary and 8 bytes past one (the 8-byte form), on a
+    15 x 14 periodic hex mesh."""
+    torch = pytest.importorskip("torch")
+    import mpaso.gpu as G
+    from mpaso.initial import sw_state
+    mesh = mpaso.Mesh.hex(15, 14, 10e3, 1e-4)
+    h, u, tr = sw_state(mesh, 7, 1, 1)
+
+    def state():
+        dm = G.DeviceMesh(mesh)
+        return dm, G.State(dm, nlev=1, ntr=1, nu=1e3)
+
+    def pinned(a):
+        buf = torch.empty(a.size + offset, dtype=torch.float64).pin_memory()
+        v = buf[offset:].view(a.shape)
+        v.copy_(torch.from_numpy(np.ascontiguousarray(a)))
+        return v
+
+    _, st = state()
+    hh, uu, tt = h.copy(), u.copy(), tr.copy()
+    st.step_host(30.0, 2, hh, uu, tt)
+    _, st2 = state()
+    hp, up, tp = pinned(h), pinned(u), pinned(tr)
+    assert (hp.data_ptr() % 16 == 8) == (offset == 1)
+    st2.step_host(30.0, 2, hp, up, tp)
+    assert not np.array_equal(hh, h)
+    for a, b in ((hp, hh), (up, uu), (tp, tt)):
+        assert np.array_equal(a.numpy(), b)
+
+
 def test_async_host_boundary_calls_in_a_loop():
     """Queued one-step exchanges on the same page-locked buffers (each copying in
     what the previous one copied out) end where the same number of blocking
