@@ -4,9 +4,11 @@
   Builds anywhere (also on the GPU host, where it is the CPU baseline).
 - oracle/_ref/libref_L<L>_T<T>.so: the reference's own task sources compiled
   unmodified, where they lie under the reference checkout, against the header
-  shim in oracle/shim/, plus ref_driver.cc.  Built only when the reference
-  checkout is present (MPASO_REFERENCE_DIR, default /root/reference); the
-  outputs are git-ignored.
+  shim in oracle/shim/, plus ref_driver.cc.  Beside the checkout
+  (MPASO_REFERENCE_DIR, default /root/reference) each translation unit is
+  first amalgamated with the headers it includes into oracle/_ref/refsrc/;
+  the libraries are compiled from those units, which also lets a host without
+  the checkout build them.  All outputs are git-ignored.
 
 Usage: python oracle/build.py [--force]
 """
@@ -53,15 +55,35 @@ def ref_available():
     return all(os.path.exists(os.path.join(REF, s)) for s in REF_SOURCES)
 
 
+REF_UNIT_DIR = os.path.join(HERE, "_ref", "refsrc")  # the reference builds' translation units, amalgamated
+REF_UNITS = [s.replace("/", "_") for s in REF_SOURCES] + ["ref_driver.cc"]
+
+
+def ref_units():
+    """Paths of the reference builds' translation units (REF_SOURCES and
+    ref_driver.cc, each amalgamated with the shim and reference headers it
+    includes), written beside the checkout; None where neither the checkout
+    nor the units are present."""
+    if ref_available():
+        os.makedirs(REF_UNIT_DIR, exist_ok=True)
+        srcs = [os.path.join(REF, s) for s in REF_SOURCES] + [os.path.join(HERE, "ref_driver.cc")]
+        for name, src in zip(REF_UNITS, srcs):
+            _write_if_changed(os.path.join(REF_UNIT_DIR, name), amalgamate(src, [os.path.join(HERE, "shim"), REF, HERE],
+                                                                             _label))
+    units = [os.path.join(REF_UNIT_DIR, n) for n in REF_UNITS]
+    return units if all(os.path.exists(u) for u in units) else None
+
+
 def build_ref(force=False):
-    """Returns {(L, T): path} for the reference builds (empty if no checkout)."""
-    if not ref_available():
+    """Returns {(L, T): path} for the reference builds (empty without the
+    checkout or its amalgamated units): the reference's task sources, compiled
+    from the units, so a host without the checkout (the GPU host) builds the
+    same libraries from the units made beside one."""
+    units = ref_units()
+    if units is None:
         return {}
     out_dir = os.path.join(HERE, "_ref")
-    os.makedirs(out_dir, exist_ok=True)
-    shim = os.path.join(HERE, "shim")
-    shim_deps = [os.path.join(dp, f) for dp, _, fs in os.walk(shim) for f in fs]
-    deps = shim_deps + [os.path.join(HERE, f) for f in ("ref_driver.cc", "sw_extra.c", "oracle.h", "build.py")]
+    deps = units + [os.path.join(HERE, f) for f in ("sw_extra.c", "oracle.h", "build.py")]
 
     def one(cfg):
         L, T = cfg
@@ -70,11 +92,9 @@ def build_ref(force=False):
             return cfg, out
         defs = [f"-DMPASO_REF_NVL={L}", f"-DMPASO_REF_NTR={T}", f"-DMPASO_REF_GRAVITY={GRAVITY}"]
         objs = []
-        for src in REF_SOURCES + ["ref_driver.cc"]:
-            path = os.path.join(REF, src) if src in REF_SOURCES else os.path.join(HERE, src)
-            obj = os.path.join(out_dir, f"L{L}_T{T}_" + src.replace("/", "_") + ".o")
-            _run(["g++", "-std=c++17", *CFLAGS, *defs, f"-I{shim}", f"-I{REF}", f"-I{HERE}",
-                  "-w", "-c", path, "-o", obj])
+        for u in units:
+            obj = os.path.join(out_dir, f"L{L}_T{T}_" + os.path.basename(u) + ".o")
+            _run(["g++", "-std=c++17", *CFLAGS, *defs, "-w", "-c", u, "-o", obj])
             objs.append(obj)
         obj = os.path.join(out_dir, f"L{L}_T{T}_sw_extra.o")
         _run(["gcc", "-std=c11", *CFLAGS, f"-I{HERE}", "-c", os.path.join(HERE, "sw_extra.c"), "-o", obj])
@@ -87,6 +107,15 @@ def build_ref(force=False):
         out = dict(ex.map(one, REF_CONFIGS))
         out["cstep"] = cstep.result()
         return out
+
+
+def _label(p):
+    """Name of a file in the #line directives of an amalgamated unit."""
+    p = os.path.realpath(p)
+    for base, name in ((os.path.realpath(REF), "reference"), (os.path.realpath(os.path.dirname(HERE)), ".")):
+        if p.startswith(base + os.sep):
+            return os.path.join(name, os.path.relpath(p, base))
+    return os.path.basename(p)
 
 
 _INCLUDE = re.compile(r'^\s*#\s*include\s*([<"])([^>"]+)[>"]')
@@ -168,16 +197,8 @@ def build_flecsi_wrappers(force=False):
                 os.path.join(HERE, "flecsi_probe.cc"), os.path.join(wrap, "sw_tasks.cc"),
                 os.path.join(wrap, "ocean_tasks.cc")]
         dirs = [os.path.join(HERE, "shim"), REF, HERE, wrap, os.path.join(root, "include")]
-
-        def label(p):
-            p = os.path.realpath(p)
-            for base, name in ((os.path.realpath(REF), "reference"), (os.path.realpath(root), ".")):
-                if p.startswith(base + os.sep):
-                    return os.path.join(name, os.path.relpath(p, base))
-            return os.path.basename(p)
-
         for name, src in zip(FLW_UNITS, srcs):
-            _write_if_changed(os.path.join(FLW_DIR, name), amalgamate(src, dirs, label))
+            _write_if_changed(os.path.join(FLW_DIR, name), amalgamate(src, dirs, _label))
     units = [os.path.join(FLW_DIR, n) for n in FLW_UNITS]
     if not all(os.path.exists(u) for u in units):
         return None
