@@ -48,9 +48,23 @@
 
 namespace mpaso {
 
+// One set of tape arrays (a segment's stage states and intermediates).
+struct TapeSet {
+  double *u, *h, *pv, *hs, *s1, *tr, *A, *LO, *tLO, *hpi;
+  double2 *R2;
+};
+
 struct AdjBuffers {
   void *arena = nullptr;
   size_t bytes = 0;
+  // two tape sets on meshes too small to fill the GPU: the reverse sweep
+  // recomputes segment s - 1 into one on a side stream while it reverses
+  // segment s from the other (`tape[1]` unused otherwise); the tp_* pointers
+  // below are the set in use
+  bool dbl = false;
+  TapeSet tape[2] = {};
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_tape = nullptr, ev_rev = nullptr;
   int N = 0, k = 0, nck = 0, cap_ck = 0, cap_k = 0;
   double dt = 0.0;
   bool have_forward = false;
@@ -112,6 +126,9 @@ void free_adjoint(SwState &s) {
   if (s.adj) {
     drop_adjoint_graph(s);
     if (s.adj->arena) cudaFree(s.adj->arena);
+    for (cudaEvent_t e : {s.adj->ev_fork, s.adj->ev_tape, s.adj->ev_rev})
+      if (e) cudaEventDestroy(e);
+    if (s.adj->side) cudaStreamDestroy(s.adj->side);
     delete s.adj;
     s.adj = nullptr;
   }
@@ -733,10 +750,14 @@ void ensure_buffers(SwState &s, int N, int k) {
   const DMesh &m = s.mesh->ctx.d;
   const int64_t L = s.L, eu = (int64_t)m.nE * L, ch = (int64_t)m.nC * L, vv = (int64_t)m.nV * L;
   const int nck = (N + k - 1) / k + 1;
+  // a second tape set where the window has two segments or more and the
+  // stages leave most of the GPU idle (under 2^20 cell-levels)
+  const bool dbl = k < N && (int64_t)m.nC * L < (1LL << 20);
   AdjBuffers *A = s.adj;
-  if (A && A->cap_ck >= nck && A->cap_k >= k) return;
+  if (A && A->cap_ck >= nck && A->cap_k >= k && (A->dbl || !dbl)) return;
   free_adjoint(s);
   A = s.adj = new AdjBuffers();
+  A->dbl = dbl;
   // the ocean app differentiates its tracers only: no (h, u) tape or cotangents
   const int64_t hu = s.p.app == MPASO_APP_OCEAN ? 0 : 1;
   std::vector<std::pair<double **, int64_t>> bufs = {
@@ -758,6 +779,20 @@ void ensure_buffers(SwState &s, int N, int k) {
         {&A->lhet, hu * eu}, {(double **)&A->lho, 2 * eT}, {(double **)&A->p12, 2 * eT}};
     bufs.insert(bufs.end(), tb.begin(), tb.end());
   }
+  TapeSet &t1 = A->tape[1];
+  if (dbl) {
+    const std::vector<std::pair<double **, int64_t>> tb = {
+        {&t1.u, hu * (4LL * k + 1) * eu}, {&t1.h, hu * (4LL * k + 1) * ch}, {&t1.pv, hu * (4LL * k + 1) * vv},
+        {&t1.hs, hu * (4LL * k + 1) * vv}, {&t1.s1, hu * 4LL * k * eu}};
+    bufs.insert(bufs.end(), tb.begin(), tb.end());
+    if (s.T > 0) {
+      const int64_t cT = ch * s.T, eT = eu * s.T;
+      const std::vector<std::pair<double **, int64_t>> tt = {
+          {&t1.tr, (4LL * k + 1) * cT}, {&t1.A, 4LL * k * eT}, {&t1.LO, 4LL * k * eT},
+          {(double **)&t1.R2, 8LL * k * cT}, {&t1.tLO, 4LL * k * cT}, {&t1.hpi, hu * 4LL * k * ch}};
+      bufs.insert(bufs.end(), tt.begin(), tt.end());
+    }
+  }
   size_t total = 0;
   for (auto &b : bufs) total += ((size_t)std::max<int64_t>(b.second, 1) * 8 + 255) & ~size_t(255);
   if (cudaMalloc(&A->arena, total) != cudaSuccess) {
@@ -772,8 +807,22 @@ void ensure_buffers(SwState &s, int N, int k) {
     *b.first = (double *)p;
     p += ((size_t)std::max<int64_t>(b.second, 1) * 8 + 255) & ~size_t(255);
   }
+  A->tape[0] = TapeSet{A->tp_u, A->tp_h, A->tp_pv, A->tp_hs, A->tp_s1, A->tp_tr,
+                       A->tp_A, A->tp_LO, A->tp_tLO, A->tp_hpi, A->tp_R2};
+  if (dbl) {
+    MPASO_CUDA(cudaStreamCreateWithFlags(&A->side, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&A->ev_fork, &A->ev_tape, &A->ev_rev})
+      MPASO_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
   A->cap_ck = nck;
   A->cap_k = k;
+}
+
+// Makes tape set b the one the tp_* pointers name.
+void use_tape(AdjBuffers &A, int b) {
+  const TapeSet &t = A.tape[b];
+  A.tp_u = t.u, A.tp_h = t.h, A.tp_pv = t.pv, A.tp_hs = t.hs, A.tp_s1 = t.s1, A.tp_tr = t.tr;
+  A.tp_A = t.A, A.tp_LO = t.LO, A.tp_tLO = t.tLO, A.tp_hpi = t.hpi, A.tp_R2 = t.R2;
 }
 
 // Reverse of the stage whose input state is tape slot j; `first`: no B3 before
@@ -930,6 +979,7 @@ void forward(SwState &s, double dt, int N, int k) {
   if (stored) k = N;
   ensure_buffers(s, N, k);
   AdjBuffers &A = *s.adj;
+  use_tape(A, 0);
   A.stored = stored;
   if (stored) {
     A.N = N, A.k = N, A.dt = dt, A.nck = 1;
@@ -1054,20 +1104,51 @@ void reverse_body(SwState &s) {
   const int64_t cT = ch * s.T;
   const cudaStream_t st = s.stream;
   const bool ocean = s.p.app == MPASO_APP_OCEAN;
+  // With two tape sets, segment seg's tape is set (nck - 1 - seg) mod 2 (the
+  // last segment in set 0, where the checkpointing forward tapes it), and the
+  // side stream recomputes segment seg - 1 while this stream reverses segment
+  // seg: the reverse reads only its tape set and its own buffers, the
+  // recompute only writes the other set and the forward's scratch, and no two
+  // recomputes run at once.
+  const bool dbl = A.dbl && !A.stored && A.nck > 1;
+  auto set_of = [&](int seg) { return dbl ? (A.nck - 1 - seg) & 1 : 0; };
+  auto recompute = [&](int seg, cudaStream_t q) {  // taping recompute of a segment from its checkpoint
+    const int n = std::min(A.k, A.N - seg * A.k);
+    if (!ocean) {
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, q));
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, q));
+    }
+    if (A.tr)
+      MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, q));
+    tape_segment(s, A, n, A.tr != 0, q);
+  };
   if (ocean) ocean_recompute(s, A.dt, st);  // the prescribed flux and 1/hProv the stages used
   for (int seg = A.nck - 1; seg >= 0; --seg) {
     const int s0 = seg * A.k, n = std::min(A.k, A.N - s0);
-    if (!A.stored && !(seg == A.nck - 1 && A.rev_skip)) {
-      // taping recompute of the segment from its checkpoint
-      if (!ocean) {
-        MPASO_CUDA(cudaMemcpyAsync(A.tp_u, A.ck_u + (size_t)seg * eu, eu * 8, cudaMemcpyDeviceToDevice, st));
-        MPASO_CUDA(cudaMemcpyAsync(A.tp_h, A.ck_h + (size_t)seg * ch, ch * 8, cudaMemcpyDeviceToDevice, st));
+    const bool last = seg == A.nck - 1;
+    if (!A.stored) {
+      if (last) {
+        use_tape(A, set_of(seg));
+        if (!A.rev_skip) recompute(seg, st);
+        if (dbl) {  // the side stream joins after this stream's recompute
+          MPASO_CUDA(cudaEventRecord(A.ev_fork, st));
+          MPASO_CUDA(cudaStreamWaitEvent(A.side, A.ev_fork, 0));
+        }
+      } else if (dbl) {
+        MPASO_CUDA(cudaStreamWaitEvent(st, A.ev_tape, 0));  // this segment's tape, from the side stream
+      } else {
+        recompute(seg, st);
       }
-      if (A.tr)
-        MPASO_CUDA(cudaMemcpyAsync(A.tp_tr, A.ck_tr + (size_t)seg * cT, cT * 8, cudaMemcpyDeviceToDevice, st));
-      tape_segment(s, A, n, A.tr != 0, st);
     }
-    if (seg == A.nck - 1) {
+    if (dbl && seg >= 1) {
+      // the next segment's tape into the set the reverse of segment seg + 1 used
+      if (!last) MPASO_CUDA(cudaStreamWaitEvent(A.side, A.ev_rev, 0));
+      use_tape(A, set_of(seg - 1));
+      recompute(seg - 1, A.side);
+      MPASO_CUDA(cudaEventRecord(A.ev_tape, A.side));
+    }
+    use_tape(A, set_of(seg));
+    if (last) {
       // cotangents of the final state (tape slot 4n): tracers to q = h tr, then
       // the first reversed stage's lk = dt/6 lam
       if (A.tr && !ocean)
@@ -1086,10 +1167,13 @@ void reverse_body(SwState &s) {
         const int j = 4 * t + rk;
         tra_done = stage_vjp(s, A, rk, j, t == n - 1 && rk == 3, j > 0, st, tra_done);
       }
+    if (dbl) MPASO_CUDA(cudaEventRecord(A.ev_rev, st));
   }
-  // q = h tr at the window's start (tape slot 0 holds checkpoint 0)
+  // q = h tr at the window's start (tape slot 0 of segment 0 holds checkpoint 0)
+  use_tape(A, set_of(0));
   if (A.tr && !ocean)
     k_adj_q_convert<<<blocks_for(ch, TPB), TPB, 0, st>>>(ch, s.T, A.tp_h, A.tp_tr, A.lam_q, A.lam_h, 1);
+  use_tape(A, 0);  // the forward tapes into set 0
   MPASO_CUDA(cudaGetLastError());
 }
 
