@@ -351,7 +351,10 @@ int mpaso_state_autotune(mpaso_state s, double dt, int32_t nsteps, int32_t *conf
  * with tracers also ceil(N / ckpt_every) + 4 ckpt_every + 1 copies of the
  * tracers, 4 ckpt_every copies of two edge-tracer fields (fluxes A, LO) and
  * of the two limiter factors, and about 15 work arrays of one level-tracer
- * field. */
+ * field.  On meshes under 2^20 cell-levels with two segments or more, the
+ * 4 ckpt_every (+ 1) taped copies are held twice: the reverse sweep
+ * recomputes the next segment into the second set while it reverses the
+ * current one (same gradient, bit for bit). */
 int mpaso_rk4_forward(mpaso_state s, double dt, int32_t nsteps, int32_t ckpt_every);
 int mpaso_rk4_vjp(mpaso_state s, const double *gh, const double *gu, double *gh0, double *gu0);
 int mpaso_rk4_vjp_tracers(mpaso_state s, const double *gh, const double *gu, const double *gtr,
