@@ -9,6 +9,7 @@ host-only entry points work there) and on the GB300 machine after a rebuild.
 """
 import concurrent.futures as cf
 import hashlib
+import platform
 import os
 import shutil
 import subprocess
@@ -43,7 +44,7 @@ def _sources():
 
 
 def _digest(paths, extra):
-    h = hashlib.sha1()
+    h = hashlib.sha1(platform.machine().encode())  # objects of another host architecture never match
     for p in paths:
         with open(p, "rb") as f:
             h.update(f.read())

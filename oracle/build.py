@@ -13,6 +13,7 @@
 Usage: python oracle/build.py [--force]
 """
 import os
+import platform
 import re
 import subprocess
 import sys
@@ -34,8 +35,16 @@ def _run(cmd):
         raise RuntimeError("oracle build failed:\n" + " ".join(cmd) + "\n" + r.stderr)
 
 
+def _foreign(path):
+    """Whether the ELF file `path` was built for another machine than this host's."""
+    want = {"x86_64": 62, "aarch64": 183}.get(platform.machine())
+    with open(path, "rb") as f:
+        hdr = f.read(20)
+    return want is not None and hdr[:4] == b"\x7fELF" and int.from_bytes(hdr[18:20], "little") != want
+
+
 def _stale(out, deps):
-    if not os.path.exists(out):
+    if not os.path.exists(out) or _foreign(out):
         return True
     t = os.path.getmtime(out)
     return any(os.path.getmtime(d) > t for d in deps)
