@@ -169,10 +169,13 @@ __global__ void __launch_bounds__(TPB) k_oc_cells(DMesh m, Stage S, int L) {
       if (ok) {
         td[t] += dflip(invAreaCell1 * S.LO[ie0 + t], sm);
         const double ax = dflip(invAreaCell1 * S.A[ie0 + t], sm);
-        if (dgt0(ax))
-          fi[t] += ax;
-        else if (dlt0(ax))
-          fo[t] += ax;
+        // flxIn += max(0, ax), flxOut += min(0, ax): one add into the sum the
+        // sign selects (integer-pipe selects; a zero ax changes neither sum,
+        // so none is kept), instead of an add in each of two divergent branches
+        const bool in = dgt0(ax), out = dlt0(ax);
+        const double acc = (in ? fi[t] : fo[t]) + ax;
+        fi[t] = in ? acc : fi[t];
+        fo[t] = out ? acc : fo[t];
       }
     }
   });
@@ -223,11 +226,12 @@ __global__ void __launch_bounds__(TPB) k_oc_final(DMesh m, Stage S, int L) {
         const double a = S.A[ie0 + t];
         const double2 o = S.R2[jn + t];
         const double2 r1 = first ? own[t] : o, r2 = first ? o : own[t];  // {R+, R-} of c1, c2
-        double hl = 0.0;
-        if (dgt0(a))
-          hl = a * dmin(r1.y, r2.x);
-        else if (dlt0(a))
-          hl = a * dmin(r1.x, r2.y);
+        // one product with the minimum the sign selects (integer-pipe selects);
+        // a zero flux enters as +0, whose products are the +0 the reference's
+        // max(0, A) / min(0, A) terms give
+        const bool pos = dgt0(a);
+        const double rmin = pos ? dmin(r1.y, r2.x) : dmin(r1.x, r2.y);
+        const double hl = (dgt0(a) || dlt0(a) ? a : 0.0) * rmin;
         td[t] += dflip(invAreaCell1 * hl, sm);
       }
     });
