@@ -434,13 +434,12 @@ __device__ __forceinline__ void tr_a_item(const DMesh &m, const TrArgs &a, int L
         sel = first ? (dkey(ot.x) < dkey(own.y) ? 0 : 2) : (dkey(own.x) < dkey(ot.y) ? 1 : 0);
       else if (dlt0(aa))
         sel = first ? (dkey(ot.y) < dkey(own.x) ? 0 : 1) : (dkey(own.y) < dkey(ot.x) ? 2 : 0);
-      if (sel) {
+      if (sel) {  // one subtraction and one fma into the factor's sum (selected operands)
         const double go = a.gq[jo];
-        const double G = first ? go - gc : gc - go;  // g(c2) - g(c1)
-        if (sel == 1)
-          lrp = fma(G, aa, lrp);
-        else
-          lrm = fma(G, aa, lrm);
+        const double G = (first ? go : gc) - (first ? gc : go);  // g(c2) - g(c1)
+        const double acc = fma(G, aa, sel == 1 ? lrp : lrm);
+        lrp = sel == 1 ? acc : lrp;
+        lrm = sel == 1 ? lrm : acc;
       }
     };
     if constexpr (NL == 1)
@@ -544,21 +543,23 @@ __device__ __forceinline__ void tr_b_item(const DMesh &m, const TrArgs &a, int L
     double p1 = 0.0, p2 = 0.0;
     if (a.fct) {
       const double aa = a.A[it], lo = a.LO[it];
+      // the branch the flux sign took, as one subtraction and one fma whose
+      // operands the sign selects (integer-pipe selects, the same arithmetic
+      // per lane), so a warp with both signs issues them once
+      const bool ap = dgt0(aa), an = dlt0(aa);
       double lA = 0.0;
-      if (dgt0(aa)) {
-        const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
-        lA = fma(G, dmin(r1.y, r2.x), a.lfio[i2t].x - a.lfio[i1t].y);
-      } else if (dlt0(aa)) {
-        const double2 r1 = a.R2[i1t], r2 = a.R2[i2t];
-        lA = fma(G, dmin(r1.x, r2.y), a.lfio[i2t].y - a.lfio[i1t].x);
+      if (ap || an) {
+        const double2 r1 = a.R2[i1t], r2 = a.R2[i2t], f1 = a.lfio[i1t], f2 = a.lfio[i2t];
+        const double rmin = ap ? dmin(r1.y, r2.x) : dmin(r1.x, r2.y);
+        lA = fma(G, rmin, (ap ? f2.x : f2.y) - (ap ? f1.y : f1.x));
       }
       const double lLO = G + (a.ltl[i2t] - a.ltl[i1t]) - lA;
-      if (pos) {
-        lF = fma(lLO * dv, tr1, lF);
-        p1 = lLO * dv * F;
-      } else if (neg) {
-        lF = fma(lLO * dv, tr2, lF);
-        p2 = lLO * dv * F;
+      if (pos || neg) {  // the upwind value's cotangent, on the side the flux sign picks
+        const double q = lLO * dv;
+        lF = fma(q, pos ? tr1 : tr2, lF);
+        const double pq = q * F;
+        p1 = pos ? pq : 0.0;
+        p2 = pos ? 0.0 : pq;
       }
       double S;
       if (pos || neg) {
