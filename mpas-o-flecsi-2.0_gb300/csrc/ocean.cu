@@ -90,7 +90,9 @@ __global__ void __launch_bounds__(TPB) k_oc_edges(DMesh m, DStat st, Stage S, in
   if (S.fct) {
     const double f = S.F[i];
     const int mask = m.hoMask[(int64_t)e * m.fctLev + k];
-    const double wgt = f * (double)mask;  // wgtTmp (solve.cc:145)
+    // wgtTmp = f mask (solve.cc:145): for a mask of 1 f itself, for 0 the zero
+    // with f's sign, on the integer pipe (other masks: the product)
+    const double wgt = mask == 1 ? f : mask == 0 ? bitsd(dbits(f) & kSignBit) : f * (double)mask;
     // sgnTmp = sign(f) picks the factor coef1 + coef3 sgn; where f = 0 the
     // weight wgt is a zero and so is every weightFactor, whichever is picked
     const bool neg = dlt0(f);
@@ -112,13 +114,19 @@ __global__ void __launch_bounds__(TPB) k_oc_edges(DMesh m, DStat st, Stage S, in
     // LO = dv (max(0, f) tr1 + min(0, f) tr2): one of the two products is a zero
     const bool up1 = dgt0(f);
     // tracerWeight of solve.cc:222-223 is a zero on edges whose high-order mask
-    // is set (their high-order flux gains nothing); on the others the centred flux
-    const double tw = mask ? 0.0 : (double)((mask + 1) & 1) * (dv * 0.5) * f;
+    // is set (their high-order flux gains nothing); on the others the centred
+    // flux, with ((mask + 1) & 1) = 1.  A branch, not a select: the mask is set
+    // almost everywhere, so warps skip this work instead of issuing it
+    if (!mask) {
+      const double tw = (dv * 0.5) * f;
+#pragma unroll
+      for (int t = 0; t < T; ++t) flx[t] = flx[t] + tw * (t1[t] + t2[t]);
+    }
 #pragma unroll
     for (int t = 0; t < T; ++t) {
       const double lo = dv * (f * (up1 ? t1[t] : t2[t]));
       S.LO[i * T + t] = lo;
-      S.A[i * T + t] = (mask ? flx[t] : flx[t] + tw * (t1[t] + t2[t])) - lo;
+      S.A[i * T + t] = flx[t] - lo;
     }
   }
   if (S.hmix) {
