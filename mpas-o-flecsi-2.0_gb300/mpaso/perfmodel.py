@@ -158,18 +158,19 @@ def ocean_kernels(d: Dims, fct=True, hmix=True):
     if fct:
         # F, advCells + one coefficient pair per slot, hoMask, dv, LO, A
         b1 += 8 * el + 20 * Na * nE + 4 * el + 8 * nE + 16 * el * T
-        # wgt, a weight per slot, per tracer a multiply and an add per slot, LO (2),
-        # A (1), the centred-flux weight (3)
-        f1 += el * (1 + Na + 3 + T * (2 * Na + 3))
+        # a weight per slot, per tracer a multiply and an add per slot, LO (2) and
+        # A (1); the mask weight is a select, the centred flux of unmasked edges rare
+        f1 += el * (Na + T * (2 * Na + 3))
     if hmix:
         b1 += 8 * nE + 8 * el + 8 * el * T  # rho, hE, DF
         f1 += el * 3 * T
     b2 = 4 * nC + 12 * slot_c + 8 * nC + 8 * cl * 2 + 4 * slot_c + 8 * slot_c + 8 * cl * T
     b2 += 16 * el * T + 24 * cl * T
     # per slot and tracer: LO and A scaled by 1/area and summed (4); trUp (4), the
-    # new max / min (6), numerators and denominators (6), the two quotients where
-    # a bound is active (about a quarter of the cells)
-    f2 = cl * T * (4 * Nc + 16 + 5) if fct else 0
+    # new max / min (6), numerators and denominators (6); the two quotients are
+    # divided only strictly inside (0, 1), rarely (~1 instruction per cell-level
+    # and tracer on average, from ncu's DFMA count)
+    f2 = cl * T * (4 * Nc + 16 + 1) if fct else 0
     b3 = 4 * nC + 12 * slot_c + 8 * nC + 16 * cl * T + 8 * cl * T * 3 + 16 * cl * T
     b3 += 8 * el * T * (int(fct) + int(hmix))
     # per slot and tracer: the limited flux, its 1/area scaling and sum (3), the
