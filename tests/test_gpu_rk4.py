@@ -215,6 +215,24 @@ def test_page_locked_exchange_odd_sizes_and_unaligned_buffers(offset):
         assert np.array_equal(a.numpy(), b)
 
 
+def test_ocean_host_exchange_matches_goldens():
+    """The ocean app through the host-buffer call: thickness, velocity and
+    tracers in from page-locked buffers (the one-pass exchange kernels), one
+    step at a time, equal to the reference's goldens value for value after 1
+    and 10 steps (the ocean kernels keep the reference's rounding)."""
+    torch = pytest.importorskip("torch")
+    g = Golden("ocean_icosa3_L3T2")
+    _, st = make_state(g)
+    hp, up, tp = (torch.from_numpy(np.ascontiguousarray(g[k])).pin_memory() for k in ("h0", "u0", "tr0"))
+    done = 0
+    for n in g.steps:
+        for _ in range(n - done):
+            st.step_host(g.dt, 1, hp, up, tp)
+        done = n
+        assert np.array_equal(tp.numpy(), g[f"tr_{n}"])
+        assert np.array_equal(hp.numpy(), g["h0"]) and np.array_equal(up.numpy(), g["u0"])  # prescribed
+
+
 def test_async_host_boundary_calls_in_a_loop():
     """Queued one-step exchanges on the same page-locked buffers (each copying in
     what the previous one copied out) end where the same number of blocking
