@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: builds the CPU oracle libraries.
 
 - oracle/_build/liboracle.so: the plain-C restatement (oracle.c + sw_extra.c).
-  Builds anywhere (also on the GPU host, where it is the CPU baseline).
+  Builds anywhere from this repository alone.
 - oracle/_ref/libref_L<L>_T<T>.so: the reference's own task sources compiled
   unmodified, where they lie under the reference checkout, against the header
   shim in oracle/shim/, plus ref_driver.cc.  Beside the checkout
@@ -86,8 +86,8 @@ def ref_units():
 def build_ref(force=False):
     """Returns {(L, T): path} for the reference builds (empty without the
     checkout or its amalgamated units): the reference's task sources, compiled
-    from the units, so a host without the checkout (the GPU host) builds the
-    same libraries from the units made beside one."""
+    from the units, so a host without the checkout builds the same libraries
+    from the units made beside one."""
     units = ref_units()
     if units is None:
         return {}
@@ -192,8 +192,8 @@ def build_flecsi_wrappers(force=False):
     Two steps.  Where the reference checkout is present, each translation unit
     is amalgamated (its reference, shim and wrapper headers inlined) into
     oracle/_ref/flw/, a git-ignored build output like the libraries.  The
-    units are then compiled from there, so a host without the checkout (the
-    GPU host) builds the library from the units made beside one.  None when
+    units are then compiled from there, so a host without the checkout builds
+    the library from the units made beside one.  None when
     neither the checkout nor the units are there."""
     pkg = os.path.join(os.path.dirname(HERE), "mpas-o-flecsi-2.0_gb300")
     wrap = os.path.join(pkg, "flecsi")

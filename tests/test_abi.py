@@ -33,7 +33,7 @@ def test_library_exports_every_declared_function():
 def test_no_device_is_reported_cleanly():
     import mpaso.gpu as G
     if G.device_count() > 0:
-        return  # on a GPU host this test has nothing to check
+        return  # with a device present this test has nothing to check
     n = ctypes.c_int32(7)
     assert lib().mpaso_device_count(ctypes.byref(n)) == 0 and n.value == 0
     out = ctypes.c_void_p()
