@@ -13,7 +13,7 @@
  *     helper1d::write_timestep (mpasoflecsi/io/helpers.hh:127-151), which
  *     write one record per output time along the Time dimension.
  * HDF5-based netCDF-4 files (what the reference opens with H5Fopen) need
- * libhdf5, which this build does not link; `nccopy -k cdf5 in.nc out.nc`
+ * libhdf5, which libmpaso does not link; `nccopy -k cdf5 in.nc out.nc`
  * converts them.  Host code only: no GPU needed.
  *
  * All functions return MPASO_OK or an MPASO_ERR_* code (mpaso_mesh.h); the

@@ -3,8 +3,8 @@
  *
  * The reference reads MPAS meshes from HDF5 files (mpasoflecsi/specialization/
  * definition.hh:1055-1106) and computes the FCT / del2 static coefficients on
- * the host once (apps/ocean/tasks/init_functions.cc:18-447).  HDF5 is not part
- * of this build, so libmpaso generates the same MPAS mesh datasets in memory:
+ * the host once (apps/ocean/tasks/init_functions.cc:18-447).  libmpaso does not
+ * link HDF5, so it generates the same MPAS mesh datasets in memory:
  *
  *   - a quasi-uniform sphere, the Voronoi dual of a recursively bisected
  *     icosahedron (10*4^level + 2 cells);

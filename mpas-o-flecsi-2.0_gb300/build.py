@@ -5,7 +5,8 @@ Usage: python mpas-o-flecsi-2.0_gb300/build.py [--force]
 Sources under csrc/: *.cc are compiled with g++, *.cu with nvcc for
 sm_103a only; everything is linked by nvcc into lib/libmpaso.so with the CUDA
 runtime linked statically, so the library loads on hosts without a GPU (its
-host-only entry points work there) and on the GB300 machine after a rebuild.
+host-only entry points work there) and on a GB300 host after a rebuild for its
+architecture.
 """
 import concurrent.futures as cf
 import hashlib
