@@ -97,8 +97,9 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             # advCells + the one coefficient the flux sign selects (the {cp, cm} pair the kernel
             # loads is 8 B more per slot), hoMask, LO, A
             b1 += 12 * Na * nE + 4 * el + 16 * el * T
-            # stencil sum, LO, HO, A and the centred fallback (selected, not branched) per tracer
-            f1 += el * (1 + T * (Na + 5))
+            # per tracer the stencil sum, LO and A (the centred flux of unmasked edges
+            # sits behind a branch and is rare)
+            f1 += el * T * (Na + 2)
         else:
             b1 += 8 * el * T
             f1 += el * (1 + 2 * T)
@@ -121,8 +122,9 @@ def sw_kernels(d: Dims, fct=True, hmix=True, visc=True):
             b2 += 4 * slot_c + 8 * cl * T + 16 * el * T + 24 * cl * T
             # 1/hProv (5), dt/area, dt/(area hProv); per tracer 2 sums per edge (the upwind
             # sum, and flxIn or flxOut by the flux sign), trUp (3), numerators / denominators
-            # (4), two guarded quotients (10, a quarter of the cells)
-            f2 += cl * (7 + T * (2 * Nc + 7 + 2.5))
+            # (4); the two quotients are divided only strictly inside (0, 1), rarely (about
+            # half an instruction per cell on average, from ncu's count)
+            f2 += cl * (7 + T * (2 * Nc + 7 + 0.5))
         else:
             b2 += 8 * el * T + 8 * cl * T
             f2 += cl * T * Nc

@@ -35,3 +35,22 @@ def test_dataflow_bytes_by_hand_on_a_small_mesh():
     assert dataflow_bytes(mesh, L, 0, f) == 4 * (static + L * (40 * (nC + nE) + 16 * (nV + nC)))
     assert np.isclose(dataflow_bytes(mesh, 1, 1, f, fct=False, hmix=False),
                       4 * (static + 40 * (nC + nE) + 16 * (nV + nC) + 40 * nC))
+
+
+def test_fp64_instruction_counts_match_the_profiler():
+    """The FP64 instruction counts behind the bench line's `fp64` objects, at
+    the sizes the committed ncu captures were taken on: the sw stage kernels on
+    the level-7 sphere with one FCT tracer (per launch, within 2% of ncu's
+    DFMA + DADD + DMUL counts), and the ocean's edge and final kernels on the
+    level-6 sphere with 60 levels and 3 tracers (equal to ncu's counts)."""
+    from mpaso.perfmodel import Dims, ocean_kernels, sw_kernels
+    m7 = mpaso.Mesh.icosa(7)
+    sw = sw_kernels(Dims.of(m7, 1, 1, fct_statics(m7, 1)), True, True, True)
+    ncu_sw = {"sw_edge_pre": 9830399, "sw_tend": 20152406, "sw_final": 10977361}  # profiles/*_sw_l7.txt
+    for k, v in ncu_sw.items():
+        assert abs(sw[k][1] / v - 1) < 0.025, (k, sw[k][1], v)
+    m6 = mpaso.Mesh.icosa(6)
+    oc = ocean_kernels(Dims.of(m6, 60, 3, fct_statics(m6, 60)))
+    assert int(oc["oc_edges"][1]) == 648806400  # profiles/oc_edges_ocean_l6.txt: 648,806,401
+    assert int(oc["oc_final"][1]) == 250676640  # profiles/oc_final_ocean_l6.txt: 250,676,640
+    assert abs(oc["oc_cells"][1] / 291282365 - 1) < 0.05  # the guarded divisions, averaged
